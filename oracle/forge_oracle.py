@@ -1,0 +1,952 @@
+"""CPU oracle for FORGE's real-space Hartree-Fock SCF (TEST INFRASTRUCTURE ONLY).
+
+This module restates, in numpy + scipy LAPACK, the reference algorithm of
+forge-team/forge (Fortran 90 / OpenMP / MKL).  It is the checker for the CUDA
+path in ``forge_gb300``: only ``tests/``, ``__graft_entry__.smoke()`` and the
+``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import it.  It
+is never the thing measured on the GPU path and never a fallback for it.
+
+Parity status: **parity unpinned by the reference itself.**  The reference
+ships no tests, golden vectors or fixtures, and it cannot be compiled here (no
+Fortran compiler in this image or on the GPU host; its sources do not travel
+to the GPU host).  The restatement is pinned instead by (1) a second,
+independent restatement of the pair tables and energies in C
+(``oracle/forge_oracle_c.c``) that must agree to rounding, (2) algebraic
+invariants of the reference (Tr P(0), Hermiticity of H(k), the P(-R)=P(R)^H
+storage convention, the exactly quadratic ODA energy), and (3) integer index
+maps (neighbour cells, k grid, site maps) that are fixed by the reference's
+loops.
+
+Every function cites the reference file:line it follows.  Arrays follow the
+reference's Fortran layout where it matters (0-based in Python):
+``P[c, i, j]`` is ``zFock(i+1, j+1, c+1)``; ``coords[i, :]`` is
+``Coords(i+1, :)``.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import Optional
+
+import numpy as np
+
+F32_1EM6 = float(np.float32(1e-6))  # the default-real literal ``1e-6`` of Geometry.f90:154
+
+
+# ---------------------------------------------------------------------------
+# Setup (Setup.f90:6-74)
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class Setup:
+    """Runtime mirror of the compile-time parameters of Setup.f90:6-74.
+
+    Only the parameters that the Hartree-Fock path reads are kept; names
+    follow the reference.  ``degfactor_mode`` selects how partially occupied
+    degenerate states are weighted in GetFock: ``"reference"`` reproduces
+    ``zdeg = cmplx(DegFactor, dp)`` (HartreeFock.f90:529) literally, i.e. the
+    single-precision real part and an imaginary part equal to ``dp`` = 8;
+    ``"corrected"`` uses the real weight DegFactor.
+    """
+
+    ntheta: int = 5
+    nlayers: int = 2
+    RotateLayers: tuple = (-1, 1)
+    numk: int = 6
+    nfilling: float = 0.0
+    U: float = 4.0
+    epsilon: float = 10.0
+    Delta: float = 0.0
+    numI: int = 1
+    numC: int = 3
+    nscreen: int = 2
+    xi: float = 10.0 / 0.246
+    fphase: int = 0
+    itmax: int = 2
+    EnergyTolerance: float = 0.0001
+    StepAlternative: float = 1.0
+    pressure: float = 1.0
+    numS: int = 1
+    degfactor_mode: str = "reference"
+
+    # derived (Setup.f90:10, 23-24, 58-69)
+    @property
+    def ndim(self) -> int:
+        m = self.ntheta
+        return self.nlayers * 2 * (m * m + (m + 1) ** 2 + (m + 1) * m)
+
+    @property
+    def numb(self) -> int:
+        return min(20, self.ndim)
+
+    @property
+    def ncb(self) -> int:
+        return self.numb // 2
+
+    @property
+    def nLower(self) -> int:
+        return (self.ndim - 2 * self.numb + 2 * self.ncb) // 2 + 1
+
+    @property
+    def nUpper(self) -> int:
+        return (self.ndim + 2 * self.ncb) // 2
+
+    @property
+    def NeutralityPoint(self) -> int:
+        return (self.ndim // 2 - self.nLower) + 1
+
+    @property
+    def Nk(self) -> int:
+        return self.numk * self.numk
+
+    @property
+    def alpha(self) -> float:
+        return 5.853 / self.epsilon * 1.0
+
+    @property
+    def alphaH(self) -> float:
+        return 5.853 / self.epsilon * 1.0
+
+    @property
+    def a0(self) -> float:
+        return 1.0 / math.sqrt(3.0)
+
+    @property
+    def r0(self) -> float:
+        return 0.184
+
+    @property
+    def d0(self) -> float:
+        return 1.35772 / self.pressure
+
+    @property
+    def tz(self) -> float:
+        return 1.35772 / self.pressure
+
+
+A1 = (0.5, math.sqrt(3.0) * 0.5)   # Setup.f90:71
+A2 = (-0.5, math.sqrt(3.0) * 0.5)  # Setup.f90:72
+PI = 4.0 * math.atan(1.0)          # Setup.f90:74
+
+
+# ---------------------------------------------------------------------------
+# Geometry (Geometry.f90, Main.f90:123-163)
+# ---------------------------------------------------------------------------
+def number_neighbor_cells(numI: int) -> int:
+    """Geometry.f90:14-35."""
+    cnt = 0
+    for n1 in range(-numI, numI + 1):
+        for n2 in range(-numI, numI + 1):
+            if -numI <= n1 + n2 <= numI and (n1 != 0 or n2 != 0):
+                cnt += 1
+    return cnt // 2 + 1
+
+
+def order_neighbor_cells(numI: int, nnc: int):
+    """Geometry.f90:40-91: R list (0,0),(-1,0),(-1,1),(0,-1),... ."""
+    u1 = [0] * nnc
+    u2 = [0] * nnc
+    icount = 0
+    if numI > 0:
+        for a, b in ((-1, 0), (-1, 1), (0, -1)):
+            icount += 1
+            u1[icount], u2[icount] = a, b
+    if numI > 1:
+        for n1 in range(-numI, numI + 1):
+            for n2 in range(-numI, numI + 1):
+                if -numI <= n1 + n2 <= numI and icount < nnc - 1:
+                    if n1 != 0 or n2 != 0:
+                        icount += 1
+                        u1[icount], u2[icount] = n1, n2
+                        if (n1, n2) in ((-1, 0), (-1, 1), (0, -1)):
+                            icount -= 1
+    return np.array(u1, dtype=np.int64), np.array(u2, dtype=np.int64)
+
+
+def sample_bz(numk: int, g1, g2):
+    """Geometry.f90:96-127. Returns (nMomentaComponents[Nk,2], nMomentaFlattened, MomentaValues[numk,numk,2])."""
+    comps = np.zeros((numk * numk, 2), dtype=np.int64)
+    flat = np.zeros((numk, numk), dtype=np.int64)
+    icount = 0
+    for ivk1 in range(numk):
+        for ivk2 in range(numk):
+            icount += 1
+            comps[icount - 1] = (ivk1, ivk2)
+            flat[ivk1, ivk2] = icount
+    vals = np.zeros((numk, numk, 2))
+    for ivk2 in range(numk):
+        for ivk1 in range(numk):
+            vals[ivk1, ivk2, 0] = (ivk1 * g1[0] + ivk2 * g2[0]) / float(numk)
+            vals[ivk1, ivk2, 1] = (ivk1 * g1[1] + ivk2 * g2[1]) / float(numk)
+    return comps, flat, vals
+
+
+def _ws_accept(x1: float, x2: float, m: int, rmax: float) -> bool:
+    r1 = abs(x1 * (3.0 * m + 1) + x2 * (3.0 * m + 2)) + F32_1EM6
+    r2 = abs(x1 - x2 * (3.0 * m + 1)) + F32_1EM6
+    r3 = abs(x1 * (3.0 * m + 2) + x2) + F32_1EM6
+    return r1 < rmax and r2 < rmax and r3 < rmax
+
+
+def wigner_seitz_cell(s: Setup, t1, t2, cs: float, sn: float) -> np.ndarray:
+    """Geometry.f90:132-273: site coordinates (unrotated), layer-major, A block then B block per layer."""
+    m = s.ntheta
+    nrad = 3 * m
+    rmax = 3.0 * m ** 2 + 3.0 * m + 1.0
+    sq3 = math.sqrt(3.0)
+    coords = np.zeros((s.ndim, 3))
+    rows = []
+    for nlayer in range(1, s.nlayers + 1):
+        z = (float(np.float32(nlayer - 1)) - float(np.float32(s.nlayers - 1)) / 2.0) * s.tz
+        rot = s.RotateLayers[nlayer - 1]
+        if rot == -1:
+            for n1 in range(-nrad, nrad + 1):
+                for n2 in range(-nrad, nrad + 1):
+                    an1 = n1 + 1.0 / 3.0
+                    an2 = n2 - 2.0 / 3.0
+                    if _ws_accept(an1, an2, m, rmax):
+                        rows.append(((n1 + 1.0 / 3.0) * A1[0] + (n2 - 2.0 / 3.0) * A2[0],
+                                     (n1 + 1.0 / 3.0) * A1[1] + (n2 - 2.0 / 3.0) * A2[1], z))
+            rows.append(((-t2[0] - t1[0]) / 3.0, (-t2[1] - t1[1]) / 3.0, z))
+            for n1 in range(-nrad, nrad + 1):
+                for n2 in range(-nrad, nrad + 1):
+                    bn1 = n1 + 2.0 / 3.0
+                    bn2 = n2 - 1.0 / 3.0
+                    if _ws_accept(bn1, bn2, m, rmax):
+                        rows.append((bn1 * A1[0] + bn2 * A2[0], bn1 * A1[1] + bn2 * A2[1], z))
+            rows.append(((t2[0] + t1[0]) / 3.0, (t2[1] + t1[1]) / 3.0, z))
+        elif rot == 1:
+            for n1 in range(-nrad, nrad + 1):
+                for n2 in range(-nrad, nrad + 1):
+                    an1 = (n1 + 1.0 / 3.0) * (cs - sn / sq3) - 2 * (n2 - 2.0 / 3.0) * sn / sq3
+                    an2 = (n2 - 2.0 / 3.0) * (cs + sn / sq3) + 2 * (n1 + 1.0 / 3.0) * sn / sq3
+                    if _ws_accept(an1, an2, m, rmax):
+                        rows.append((an1 * A1[0] + an2 * A2[0], an1 * A1[1] + an2 * A2[1], z))
+            rows.append(((t1[0] + t2[0]) / 3.0, (t1[1] + t2[1]) / 3.0, z))
+            for n1 in range(-nrad, nrad + 1):
+                for n2 in range(-nrad, nrad + 1):
+                    bn1 = (n1 + 2.0 / 3.0) * (cs - sn / sq3) - 2 * (n2 - 1.0 / 3.0) * sn / sq3
+                    bn2 = (n2 - 1.0 / 3.0) * (cs + sn / sq3) + 2 * (n1 + 2.0 / 3.0) * sn / sq3
+                    if _ws_accept(bn1, bn2, m, rmax):
+                        rows.append((bn1 * A1[0] + bn2 * A2[0], bn1 * A1[1] + bn2 * A2[1], z))
+            rows.append(((-t1[0] - t2[0]) / 3.0, (-t1[1] - t2[1]) / 3.0, z))
+        else:
+            raise ValueError("RotateLayers entries must be -1 or +1")
+    if len(rows) != s.ndim:
+        raise RuntimeError(f"Wigner-Seitz cell found {len(rows)} sites, expected ndim={s.ndim}")
+    coords[:] = np.array(rows)
+    return coords
+
+
+def _rot(R, v):
+    """matmul(RotMatrix, v) for a 2x2 column-major RotMatrix, no FMA (Main.f90:135)."""
+    return (R[0][0] * v[0] + R[0][1] * v[1], R[1][0] * v[0] + R[1][1] * v[1])
+
+
+@dataclasses.dataclass
+class Geometry:
+    coords: np.ndarray          # (N,3)
+    t1: tuple
+    t2: tuple
+    t3: tuple
+    g1: tuple
+    g12: tuple
+    ucell1: np.ndarray          # nUnitCell_1 (NNC,)
+    ucell2: np.ndarray          # nUnitCell_2 (NNC,)
+    kcomp: np.ndarray           # nMomentaComponents (Nk,2) int64
+    kflat: np.ndarray           # nMomentaFlattened (numk,numk)
+    kvals: np.ndarray           # MomentaValues (numk,numk,2)
+    c2pairs: np.ndarray         # nC2pairs, 1-based like the reference
+    c3pairs: np.ndarray         # nC3pairs, 1-based
+    c2_count: int
+    c3_count: int
+
+    @property
+    def tn(self) -> np.ndarray:
+        """reshape([t1,t2,t3],[2,3]) of Main.f90:249, as a (3,2) array of vectors."""
+        return np.array([self.t1, self.t2, self.t3])
+
+    def vk(self, icount: int) -> np.ndarray:
+        ivk1, ivk2 = self.kcomp[icount]
+        return self.kvals[ivk1, ivk2]
+
+
+def build_geometry(s: Setup) -> Geometry:
+    """Main.f90:102-163: neighbour cells, reciprocal vectors, rotation, k grid, sites, C2/C3 maps."""
+    nnc = number_neighbor_cells(s.numI)
+    u1, u2 = order_neighbor_cells(s.numI, nnc)
+    m = s.ntheta
+    aMoire = 3.0 * m ** 2 + 3.0 * m + 1.0
+    f = (4.0 * PI / 3.0) / aMoire
+    g1 = (f * (float(3 * m + 1) * A1[0] + A2[0]), f * (float(3 * m + 1) * A1[1] + A2[1]))
+    g12 = (f * (float(3 * m + 2) * A2[0] - A1[0]), f * (float(3 * m + 2) * A2[1] - A1[1]))
+    cs = 1.0 - 1.0 / (2.0 * aMoire)
+    sn = math.sqrt(1.0 - cs ** 2)
+    th = 0.5 * math.acos(cs)
+    c, sgn = math.cos(th), math.sin(th)
+    # reshape([c,-s,s,c],[2,2]) column-major: R(1,1)=c, R(2,1)=-s, R(1,2)=s, R(2,2)=c
+    R = ((c, sgn), (-sgn, c))
+    g1 = _rot(R, g1)
+    g12 = _rot(R, g12)
+    kcomp, kflat, kvals = sample_bz(s.numk, g1, g12)
+    t1 = (float(m) * A1[0] + float(m + 1) * A2[0], float(m) * A1[1] + float(m + 1) * A2[1])
+    t2 = (float(-m - 1) * A1[0] + float(2 * m + 1) * A2[0], float(-m - 1) * A1[1] + float(2 * m + 1) * A2[1])
+    coords = wigner_seitz_cell(s, t1, t2, cs, sn)
+    # Main.f90:148-150 rotates (x, y); the z coordinate is kept (the reference's
+    # assignment of the 2-vector to the 3-row is read as "rotate x,y in place").
+    for n in range(s.ndim):
+        x, y = _rot(R, (coords[n, 0], coords[n, 1]))
+        coords[n, 0], coords[n, 1] = x, y
+    t1 = _rot(R, t1)
+    t2 = _rot(R, t2)
+    t3 = (t2[0] - t1[0], t2[1] - t1[1])
+    c2, c2cnt = c2_related_points(s, coords)
+    c3, c3cnt = c3_related_points(s, coords)
+    return Geometry(coords, t1, t2, t3, g1, g12, u1, u2, kcomp, kflat, kvals, c2, c3, c2cnt, c3cnt)
+
+
+def c2_related_points(s: Setup, coords):
+    """Geometry.f90:1140-1167 (1-based map, count)."""
+    N, L = s.ndim, s.nlayers
+    pairs = np.zeros(N, dtype=np.int64)
+    cnt = 0
+    per = N // L
+    for il in range(1, L + 1):
+        for i in range(per * (il - 1) + 1, per * (il - 1) + per // 2 + 1):
+            for j in range(per * (il - 1) + per // 2 + 1, per * (il - 1) + per + 1):
+                r = math.sqrt((coords[i - 1, 0] + coords[j - 1, 0]) ** 2 + (coords[i - 1, 1] + coords[j - 1, 1]) ** 2)
+                if r < 1e-5:
+                    pairs[i - 1] = j
+                    pairs[j - 1] = i
+                    cnt += 1
+    return pairs, cnt
+
+
+def c3_related_points(s: Setup, coords):
+    """Geometry.f90:1172-1223 (1-based map, count)."""
+    N, L = s.ndim, s.nlayers
+    per = N // L
+    pairs = np.zeros(N, dtype=np.int64)
+    cnt = 0
+    sq = math.sqrt(3.0)
+    for nl in range(1, L + 1):
+        base = (nl - 1) * per
+        for lo, hi in ((base + 1, base + per // 2), (base + per // 2 + 1, base + per)):
+            for i in range(lo, hi + 1):
+                x, y = coords[i - 1, 0], coords[i - 1, 1]
+                x3 = -.5 * x - .5 * sq * y
+                y3 = .5 * sq * x - .5 * y
+                for j in range(lo, hi + 1):
+                    r = math.sqrt((coords[j - 1, 0] - x3) ** 2 + (coords[j - 1, 1] - y3) ** 2)
+                    if r < 1e-3:
+                        pairs[i - 1] = j
+                        cnt += 1
+    for nl in range(1, L + 1):
+        pairs[(nl - 1) * per + per // 2 - 1] = (nl - 1) * per + per // 2
+        pairs[(nl - 1) * per + per - 1] = (nl - 1) * per + per
+        cnt += 2
+    return pairs, cnt
+
+
+# ---------------------------------------------------------------------------
+# Model functions ft / fv (TightBinding.f90:216-230, HartreeFock.f90:1232-1274)
+# ---------------------------------------------------------------------------
+def ft(s: Setup, ri, rj):
+    """TightBinding.f90:216-230, vectorised over broadcast arrays of shape (...,3)."""
+    ri = np.asarray(ri, dtype=np.float64)
+    rj = np.asarray(rj, dtype=np.float64)
+    d = ri - rj
+    r = np.sqrt(d[..., 0] ** 2 + d[..., 1] ** 2 + d[..., 2] ** 2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        cs = d[..., 2] / r
+        val = -2.7 * np.exp((s.a0 - r) / s.r0) * (1 - cs ** 2) + 0.48 * np.exp((s.d0 - r) / s.r0) * cs ** 2
+    return np.where(r > 0.001, val, 0.0)
+
+
+def fv(s: Setup, ri, rj):
+    """HartreeFock.f90:1232-1274 (dual-gate image sum for nscreen=2, single gate for nscreen=1)."""
+    ri = np.asarray(ri, dtype=np.float64)
+    rj = np.asarray(rj, dtype=np.float64)
+    xi_, yi, zi = ri[..., 0], ri[..., 1], ri[..., 2]
+    xj, yj, zj = rj[..., 0], rj[..., 1], rj[..., 2]
+    dx, dy, dz = xi_ - xj, yi - yj, zi - zj
+    r = np.sqrt(dx * dx + dy * dy + dz * dz)
+    r2 = np.sqrt(dx * dx + dy * dy)
+    xi = s.xi
+    shape = np.broadcast(xi_, xj).shape
+    if s.nscreen == 2:
+        near = (r2 < xi) | (r2 < 2 * s.nlayers * s.tz)
+        rho2 = (xj - xi_) ** 2 + (yj - yi) ** 2
+        acc = np.zeros(shape)
+        for n in range(-20, 21):
+            sgn = 1.0 if n % 2 == 0 else -1.0
+            acc = acc + sgn / np.sqrt(rho2 + (zj - (n * xi + zi * sgn)) ** 2)
+        with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+            far = 2.0 * math.sqrt(2.0) / np.sqrt(r2 / xi) * np.exp(-PI * r2 / xi) / xi
+        out = np.where(near, acc, far)
+        return np.where(r > 0.01, out, 0.0)
+    if s.nscreen == 1:
+        with np.errstate(divide="ignore", invalid="ignore"):
+            val = 1.0 / r - 1.0 / np.sqrt(dx * dx + dy * dy + (zi + zj + xi) ** 2)
+        return np.where(r > 0.01, val, 0.0)
+    raise ValueError("nscreen must be 1 or 2")
+
+
+def cell_shift(g: Geometry, c: int) -> np.ndarray:
+    """n1*t1 + n2*t2 for neighbour cell c (0-based), as used in HartreeFock.f90:90-91."""
+    n1, n2 = int(g.ucell1[c]), int(g.ucell2[c])
+    return np.array([n1 * g.t1[0] + n2 * g.t2[0], n1 * g.t1[1] + n2 * g.t2[1]])
+
+
+def _shift_coords(coords, n1, n2, g: Geometry, sign: float):
+    """[Coords(:,1:2) -/+ n1*t1 -/+ n2*t2, Coords(:,3)] in the reference's evaluation order."""
+    out = coords.copy()
+    if sign < 0:
+        out[:, 0] = coords[:, 0] - n1 * g.t1[0] - n2 * g.t2[0]
+        out[:, 1] = coords[:, 1] - n1 * g.t1[1] - n2 * g.t2[1]
+    else:
+        out[:, 0] = coords[:, 0] + n1 * g.t1[0] + n2 * g.t2[0]
+        out[:, 1] = coords[:, 1] + n1 * g.t1[1] + n2 * g.t2[1]
+    return out
+
+
+@dataclasses.dataclass
+class PairTables:
+    """ft and fv for all orbital pairs and the 1 + 2*(NNC-1) cell images.
+
+    ``tm[c][i,j] = ft(r_i, r_j - R_c)``, ``tp[c][i,j] = ft(r_i, r_j + R_c)``;
+    same for ``vm``/``vp`` with fv.  c = 0 is R = 0 (tm[0] == tp[0]).
+    """
+
+    tm: np.ndarray
+    tp: np.ndarray
+    vm: np.ndarray
+    vp: np.ndarray
+
+
+_CLIB = None
+
+
+def _clib():
+    """Loads oracle/libforge_oracle.so (built by oracle/Makefile), or returns None."""
+    global _CLIB
+    if _CLIB is None:
+        import ctypes
+        import os
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libforge_oracle.so")
+        if not os.path.exists(path):
+            return None
+        lib = ctypes.CDLL(path)
+        lib.fo_pair_tables.restype = None
+        lib.fo_long_range.restype = None
+        lib.fo_rank1_projector.restype = None
+        _CLIB = lib
+    return _CLIB
+
+
+def _model_struct(s: Setup):
+    import ctypes
+
+    class FoModel(ctypes.Structure):
+        _fields_ = [("a0", ctypes.c_double), ("r0", ctypes.c_double), ("d0", ctypes.c_double),
+                    ("tz", ctypes.c_double), ("xi", ctypes.c_double), ("nlayers", ctypes.c_int64),
+                    ("nscreen", ctypes.c_int64)]
+    return FoModel(s.a0, s.r0, s.d0, s.tz, s.xi, s.nlayers, s.nscreen)
+
+
+def _ptr(a):
+    import ctypes
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def pair_tables(s: Setup, g: Geometry, use_c: Optional[bool] = None) -> PairTables:
+    """Tabulates the ft/fv calls of HartreeFock.f90:81-110 and 1035-1043, 1125-1133.
+
+    ``use_c`` selects the C restatement (default: when built) or the numpy one.
+    """
+    lib = _clib() if use_c in (None, True) else None
+    if use_c and lib is None:
+        raise RuntimeError("oracle/libforge_oracle.so is not built")
+    if lib is not None:
+        import ctypes
+        N = s.ndim
+        nnc = len(g.ucell1)
+        X = np.ascontiguousarray(g.coords)
+        out = [np.zeros((nnc, N, N)) for _ in range(4)]
+        u1 = np.ascontiguousarray(g.ucell1, dtype=np.int64)
+        u2 = np.ascontiguousarray(g.ucell2, dtype=np.int64)
+        t1 = np.array(g.t1)
+        t2 = np.array(g.t2)
+        mdl = _model_struct(s)
+        lib.fo_pair_tables(ctypes.c_int64(N), _ptr(X), ctypes.c_int64(nnc), _ptr(u1), _ptr(u2), _ptr(t1), _ptr(t2),
+                           ctypes.byref(mdl), *[_ptr(o) for o in out])
+        return PairTables(*out)
+    N = s.ndim
+    nnc = len(g.ucell1)
+    X = g.coords
+    tm = np.zeros((nnc, N, N))
+    tp = np.zeros((nnc, N, N))
+    vm = np.zeros((nnc, N, N))
+    vp = np.zeros((nnc, N, N))
+    ri = X[:, None, :]
+    for c in range(nnc):
+        n1, n2 = int(g.ucell1[c]), int(g.ucell2[c])
+        Xm = _shift_coords(X, n1, n2, g, -1.0)
+        Xp = _shift_coords(X, n1, n2, g, +1.0)
+        tm[c] = ft(s, ri, Xm[None, :, :])
+        tp[c] = ft(s, ri, Xp[None, :, :])
+        vm[c] = fv(s, ri, Xm[None, :, :])
+        vp[c] = fv(s, ri, Xp[None, :, :])
+    return PairTables(tm, tp, vm, vp)
+
+
+def long_range_interaction(s: Setup, g: Geometry, use_c: Optional[bool] = None) -> np.ndarray:
+    """HartreeFock.f90:14-53: LR(n,m) = sum over |n1|,|n2|,|n1+n2|<=numC of fv(r_n - n1 t1 - n2 t2, r_m)."""
+    N = s.ndim
+    lib = _clib() if use_c in (None, True) else None
+    if use_c and lib is None:
+        raise RuntimeError("oracle/libforge_oracle.so is not built")
+    if lib is not None:
+        import ctypes
+        LR = np.zeros((N, N))
+        X = np.ascontiguousarray(g.coords)
+        mdl = _model_struct(s)
+        lib.fo_long_range(ctypes.c_int64(N), _ptr(X), _ptr(np.array(g.t1)), _ptr(np.array(g.t2)),
+                          ctypes.c_int64(s.numC), ctypes.byref(mdl), _ptr(LR))
+        return LR
+    X = g.coords
+    LR = np.zeros((N, N))
+    nC = s.numC
+    for n1 in range(-nC, nC + 1):
+        for n2 in range(-nC, nC + 1):
+            if -nC <= n1 + n2 <= nC:
+                Xs = X.copy()
+                Xs[:, 0] = X[:, 0] - n1 * g.t1[0] - n2 * g.t2[0]
+                Xs[:, 1] = X[:, 1] - n1 * g.t1[1] - n2 * g.t2[1]
+                LR += fv(s, Xs[:, None, :], X[None, :, :])
+    # only m >= n is computed, then mirrored (HartreeFock.f90:28-51)
+    iu = np.triu_indices(N, 1)
+    LR.T[iu] = LR[iu]
+    return LR
+
+
+# ---------------------------------------------------------------------------
+# Hamiltonian (HartreeFock.f90:57-127)
+# ---------------------------------------------------------------------------
+def hamiltonian(s: Setup, g: Geometry, T: PairTables, potential, P, vk) -> np.ndarray:
+    """Full Hermitian H(k) whose lower triangle is the reference's zH (HartreeFock.f90:57-127).
+
+    P has shape (NNC, N, N) with P[c] = zFock(:,:,c+1).  fphase=0 makes zphase=1.
+    """
+    N = s.ndim
+    nnc = T.tm.shape[0]
+    alpha = s.alpha
+    H = np.zeros((N, N), dtype=np.complex128)
+    H += -alpha * T.vm[0] * np.conj(P[0]) + T.tm[0]
+    zs = np.zeros((N, N), dtype=np.complex128)
+    for c in range(1, nnc):
+        sh = cell_shift(g, c)
+        th = float(vk[0] * sh[0] + vk[1] * sh[1])
+        em = complex(math.cos(th), -math.sin(th))   # exp(-i k.R)
+        ep = complex(math.cos(th), math.sin(th))    # exp(+i k.R)
+        H += T.tm[c] * em + T.tp[c] * ep
+        zs += -alpha * T.vm[c] * np.conj(P[c]) * em
+        # - alpha fv(r_j, r_i - R) P(j,i) e^{+ikR}: vm[c][j,i] transposed
+        zs += -alpha * T.vm[c].T * P[c].T * ep
+    H += zs
+    if s.fphase != 0:
+        X = g.coords
+        ph = np.exp(-1j * ((X[:, None, 0] - X[None, :, 0]) * vk[0] + (X[:, None, 1] - X[None, :, 1]) * vk[1]) * s.fphase)
+        H *= ph
+    H[np.diag_indices(N)] += potential
+    if s.nlayers > 1:
+        per = N // s.nlayers
+        for n1 in range(s.nlayers):
+            H[np.arange(per) + n1 * per, np.arange(per) + n1 * per] += (n1 - (s.nlayers - 1) / 2.0) * s.Delta / (s.nlayers - 1)
+    # zH holds only the lower triangle (HartreeFock.f90:76); Hermitian completion
+    L = np.tril(H)
+    return L + np.conj(np.tril(H, -1)).T
+
+
+def eigh_lower(H: np.ndarray, nUpper: int):
+    """zdiagRed (LapackRoutines.f90:381-433): zheevr('V','I','L', il=1, iu=nUpper, abstol=dlamch('S'))."""
+    from scipy.linalg import lapack
+    n = H.shape[0]
+    safemin = np.finfo(np.float64).tiny
+    w, z, m, isuppz, info = lapack.zheevr(H, compute_v=1, range="I", lower=1, il=1, iu=nUpper,
+                                          abstol=safemin, lwork=max(65 * n, 1), lrwork=max(24 * n, 1),
+                                          liwork=max(10 * n, 1))
+    if info != 0:
+        raise RuntimeError(f"zheev failed {info}")
+    return w[:m].copy(), z[:, :m].copy()
+
+
+def bloch_phase_int(ivk1: int, ivk2: int, n1: int, n2: int, numk: int) -> complex:
+    """exp(-2 pi i (ivk1 n1 + ivk2 n1 + ivk2 n2)/numk) of HartreeFock.f90:471 and 521."""
+    th = -2.0 * PI * float(ivk1 * n1 + ivk2 * n1 + ivk2 * n2) / float(numk)
+    return complex(math.cos(th), math.sin(th))
+
+
+def solve(s: Setup, g: Geometry, T: PairTables, potential, P, keep_h=False):
+    """Solve (HartreeFock.f90:402-483).
+
+    Returns Bands (numb, Nk), zEigenvectors (N, numb, Nk), zFockBulk (NNC, N, N) (not divided by Nk),
+    plus the full eigenvalue lists of bands 1..nUpper per k.
+    """
+    N, Nk, numb = s.ndim, s.Nk, s.numb
+    nL, nU = s.nLower, s.nUpper
+    nnc = T.tm.shape[0]
+    bands = np.zeros((numb, Nk))
+    evecs = np.zeros((N, numb, Nk), dtype=np.complex128)
+    bulk = np.zeros((nnc, N, N), dtype=np.complex128)
+    allw = np.zeros((nU, Nk))
+    Hs = []
+    for ic in range(Nk):
+        ivk1, ivk2 = (int(x) for x in g.kcomp[ic])
+        vk = g.kvals[ivk1, ivk2]
+        H = hamiltonian(s, g, T, potential, P, vk)
+        if keep_h:
+            Hs.append(H.copy())
+        w, Z = eigh_lower(H, nU)
+        allw[:, ic] = w
+        bands[:, ic] = w[nL - 1:nU]
+        evecs[:, :, ic] = Z[:, nL - 1:nU]
+        if s.fphase != 0:
+            zph = np.exp(1j * (g.coords[:, 0] * vk[0] + g.coords[:, 1] * vk[1]) * s.fphase)
+        else:
+            zph = 1.0
+        occ = np.conj(Z[:, :nL - 1] * (zph if np.ndim(zph) == 0 else zph[:, None]))
+        Ck = occ @ np.conj(occ).T     # sum_n conj(psi_i) psi_j
+        bulk[0] += Ck
+        for c in range(1, nnc):
+            bulk[c] += Ck * bloch_phase_int(ivk1, ivk2, int(g.ucell1[c]), int(g.ucell2[c]), s.numk)
+    out = dict(bands=bands, evecs=evecs, bulk=bulk, eigs=allw)
+    if keep_h:
+        out["H"] = Hs
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Sorting and Fermi level
+# ---------------------------------------------------------------------------
+def dsort_lists(arr: np.ndarray) -> np.ndarray:
+    """Heap sort on column 0 of arr (rows moved together), TightBinding.f90:984-1027 (not stable)."""
+    a = [list(r) for r in np.asarray(arr, dtype=np.float64)]
+    n = len(a)
+    if n < 2:
+        return np.array(a)
+    # 1-based indexing as in the reference
+    a = [None] + a
+    l = n // 2 + 1
+    ir = n
+    while True:
+        if l > 1:
+            l -= 1
+            copy = list(a[l])
+        else:
+            copy = list(a[ir])
+            a[ir] = list(a[1])
+            ir -= 1
+            if ir == 1:
+                a[1] = copy
+                break
+        i = l
+        j = 2 * l
+        while j <= ir:
+            if j < ir and a[j][0] < a[j + 1][0]:
+                j += 1
+            if copy[0] < a[j][0]:
+                a[i] = list(a[j])
+                i = j
+                j = 2 * j
+            else:
+                j = ir + 1
+        a[i] = copy
+    return np.array(a[1:])
+
+
+def sort_energies_1spin(s: Setup, g: Geometry, bands, evecs=None):
+    """SortEnergies_1Spin (HartreeFock.f90:885-925).
+
+    Returns (sorted energies, sorted flat indices (1-based icount), nSortedMomenta, zSortedEigenvectors or None).
+    """
+    Nk, numb = s.Nk, s.numb
+    n = Nk * numb
+    e = np.zeros((n, 2))
+    for ic in range(1, n + 1):
+        indev = (ic - 1) // Nk + 1
+        e[ic - 1, 0] = bands[indev - 1, ic - (indev - 1) * Nk - 1]
+        e[ic - 1, 1] = float(ic)
+    srt = dsort_lists(e)
+    idx = np.rint(srt[:, 1]).astype(np.int64)
+    indev = (idx - 1) // Nk + 1
+    kidx = idx - (indev - 1) * Nk           # 1-based k
+    moms = g.kcomp[kidx - 1].copy()
+    sv = None
+    if evecs is not None:
+        sv = evecs[:, indev - 1, kidx - 1]
+    return srt[:, 0].copy(), idx, moms, sv, indev - 1, kidx - 1
+
+
+def fortran_nint(x: float) -> int:
+    """Fortran NINT: round half away from zero."""
+    return int(math.floor(x + 0.5)) if x >= 0 else -int(math.floor(-x + 0.5))
+
+
+def fermi_level(s: Setup, sorted_e):
+    """Main.f90:400-412: nFermiLevel, FermiEnergy, nOccStates, nPartOccStates, DegFactor."""
+    Nk = s.Nk
+    nF = s.numS * fortran_nint(float(Nk * s.NeutralityPoint) + float(Nk) / 2.0 * s.nfilling)
+    EF = (sorted_e[nF - 1] + sorted_e[nF]) / 2.0
+    tol = s.EnergyTolerance
+    nocc = 0
+    npart = 0
+    for e in sorted_e:
+        if (e - EF) < -tol:
+            nocc += 1
+        elif abs(e - EF) < tol:
+            nocc += 1
+            npart += 1
+    with np.errstate(divide="ignore", invalid="ignore"):
+        deg = np.float64(1.0) / np.float64(npart) * np.float64(nF + npart - nocc)
+    return nF, EF, nocc, npart, float(deg)
+
+
+def zdeg_weight(s: Setup, degf: float) -> complex:
+    """zdeg of HartreeFock.f90:529: cmplx(DegFactor, dp) -> real(DegFactor,4) + 8i in reference mode."""
+    if s.degfactor_mode == "reference":
+        with np.errstate(over="ignore", invalid="ignore"):
+            return complex(float(np.float32(degf)), 8.0)
+    return complex(degf, 0.0)
+
+
+def get_fock(s: Setup, g: Geometry, sorted_vecs, moms, nocc: int, npart: int, degf: float) -> np.ndarray:
+    """GetFock (HartreeFock.f90:487-560): window projector into all NNC cells (not divided by Nk)."""
+    N = s.ndim
+    nnc = len(g.ucell1)
+    out = np.zeros((nnc, N, N), dtype=np.complex128)
+    zdeg = zdeg_weight(s, degf)
+    for rng, extra in ((range(0, nocc - npart), 1.0 + 0j), (range(nocc - npart, nocc), zdeg)):
+        for nb in rng:
+            ivk1, ivk2 = (int(x) for x in moms[nb])
+            vk = g.kvals[ivk1, ivk2]
+            psi = sorted_vecs[:, nb]
+            if s.fphase != 0:
+                psi = psi * np.exp(1j * (g.coords[:, 0] * vk[0] + g.coords[:, 1] * vk[1]) * s.fphase)
+            zp = np.conj(psi)
+            outer = np.outer(zp, np.conj(zp))
+            for c in range(nnc):
+                out[c] += outer * (bloch_phase_int(ivk1, ivk2, int(g.ucell1[c]), int(g.ucell2[c]), s.numk) * extra)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Energies, ODA step, potential (HartreeFock.f90:1012-1227, Main.f90:300-342, 549-595)
+# ---------------------------------------------------------------------------
+def kinetic_energy(s: Setup, T: PairTables, P) -> float:
+    """GetKineticEnergy (HartreeFock.f90:1012-1059)."""
+    nnc = T.tm.shape[0]
+    z = np.sum(T.tm[0] * P[0])
+    for c in range(1, nnc):
+        z += np.sum(T.tm[c] * P[c]) + np.sum(T.tp[c] * np.conj(P[c].T))
+    N = P.shape[1]
+    if s.nlayers > 1 and s.Delta != 0.0:
+        per = N // s.nlayers
+        for n1 in range(s.nlayers):
+            d = np.diagonal(P[0])[n1 * per:(n1 + 1) * per]
+            z += np.sum(d) * ((n1 - (s.nlayers - 1) / 2.0) * s.Delta / (s.nlayers - 1))
+    return float(z.real)
+
+
+def fock_energy(s: Setup, T: PairTables, P) -> float:
+    """GetFockEnergy (HartreeFock.f90:1098-1145)."""
+    nnc = T.vm.shape[0]
+    z = -0.5 * np.sum(T.vm[0] * np.abs(P[0]) ** 2)
+    for c in range(1, nnc):
+        z += -0.5 * np.sum(T.vm[c] * np.abs(P[c]) ** 2) - 0.5 * np.sum(T.vp[c] * np.abs(P[c].T) ** 2)
+    return float(z)
+
+
+def hartree_hubbard_energy(LR, d1, d2):
+    """GetHartreeHubbardEnergy (HartreeFock.f90:1066-1092)."""
+    sm = d1 + d2
+    eh = 0.5 * float(sm @ LR @ sm)
+    eu = float(np.dot(d1, d2))
+    return eh, eu
+
+
+@dataclasses.dataclass
+class Energies:
+    kinetic: float
+    fock: float
+    hartree: float
+    hubbard: float
+
+    def total(self, s: Setup) -> float:
+        """Main.f90:312 / 556 for numS=1."""
+        return (s.alpha * self.fock * (3 - s.numS) + self.kinetic * (3 - s.numS)
+                + s.U * self.hubbard + s.alphaH * self.hartree)
+
+
+def energies(s: Setup, T: PairTables, LR, P, dens) -> Energies:
+    d = dens - 0.5
+    eh, eu = hartree_hubbard_energy(LR, d, d)
+    return Energies(kinetic_energy(s, T, P), fock_energy(s, T, P), eh, eu)
+
+
+def optimal_step(s: Setup, T: PairTables, LR, P_new, P_in, dens, dens_in, E_in: Energies):
+    """OptimalStep (HartreeFock.f90:1148-1227): returns (Step, energies at Step, E1, E_half)."""
+    c0 = E_in.total(s)
+    E1 = energies(s, T, LR, P_new, dens)
+    t1 = E1.total(s)
+    Eh = energies(s, T, LR, 0.5 * (P_in + P_new), .5 * (dens + dens_in))
+    t2 = Eh.total(s)
+    c1 = 4.0 * t2 - t1 - 3.0 * c0
+    c2 = t1 - c0 - c1
+    if c2 > 0 and abs(-c1 / 2.0 / c2 - .5) < 0.5:
+        step = -c1 / 2.0 / c2
+    elif t1 < c0:
+        step = 1.0
+    else:
+        step = s.StepAlternative
+    Es = energies(s, T, LR, (1.0 - step) * P_in + step * P_new, (1 - step) * dens_in + step * dens)
+    return step, Es, t1, t2
+
+
+def potential(s: Setup, LR, dens) -> np.ndarray:
+    """Main.f90:577-585 (numS=1): V_n = 2 alphaH sum_m LR(n,m)(n_m - 1/2) + U (n_n - 1/2)."""
+    d = dens - 0.5
+    return 2.0 * s.alphaH * (LR @ d) + s.U * d
+
+
+def hf_residual(s: Setup, T: PairTables, V_new, V_old, P_new, P_old) -> float:
+    """Residual of the Hartree-Fock mean field between iterations (eV).
+
+    The reference logs max|dn| and dE only (Main.f90:616-623) and stops at
+    itmax; this residual is the max over sites of |dV| and over pairs/cells of
+    alpha*|fv|*|dP|, i.e. the largest change of any H_HF matrix element.
+    """
+    dV = float(np.max(np.abs(V_new - V_old)))
+    dP = np.abs(P_new - P_old)
+    nnc = T.vm.shape[0]
+    r = 0.0
+    for c in range(nnc):
+        r = max(r, float(np.max(s.alpha * np.abs(T.vm[c]) * dP[c])))
+        if c > 0:
+            r = max(r, float(np.max(s.alpha * np.abs(T.vp[c]) * dP[c].T)))
+    return max(dV, r)
+
+
+# ---------------------------------------------------------------------------
+# SCF driver (Main.f90:236-679, numS=1, no symmetry enforcement)
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class IterationLog:
+    it: int
+    dn_max: float
+    step: float
+    dE: float
+    E_in: float
+    kin_in: float
+    fock_in: float
+    hartree_in: float
+    hubbard_in: float
+    EF: float
+    nocc: int
+    npart: int
+    residual: float
+
+
+def plain_guess(s: Setup, g: Geometry, T: PairTables):
+    """Main.f90:236-288 (nRead=0): non-interacting bands, sort, Fermi, GetFock, P=(window+bulk)/Nk."""
+    N = s.ndim
+    nnc = len(g.ucell1)
+    P0 = np.zeros((nnc, N, N), dtype=np.complex128)
+    V0 = np.zeros(N)
+    sol = solve(s, g, T, V0, P0)
+    se, _, moms, sv, _, _ = sort_energies_1spin(s, g, sol["bands"], sol["evecs"])
+    nF, EF, nocc, npart, degf = fermi_level(s, se)
+    P = get_fock(s, g, sv, moms, nocc, npart, degf)
+    P = (P + sol["bulk"]) / complex(float(s.Nk), 0.0)
+    return P, dict(sol=sol, EF=EF, nocc=nocc, npart=npart, degf=degf)
+
+
+def run_scf(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTables] = None, LR=None,
+            P_init=None, itmax: Optional[int] = None, residual_tol: Optional[float] = None,
+            keep_history: bool = False):
+    """Main.f90:236-679 for numS=1: initial guess, energies, potential, then the SCF loop with ODA mixing.
+
+    Stops after ``itmax`` iterations (reference behaviour) or earlier when
+    ``residual_tol`` is given and the mean-field residual drops below it.
+    """
+    if g is None:
+        g = build_geometry(s)
+    if T is None:
+        T = pair_tables(s, g)
+    if LR is None:
+        LR = long_range_interaction(s, g)
+    if P_init is None:
+        P, _ = plain_guess(s, g, T)
+    else:
+        P = np.array(P_init, dtype=np.complex128)
+    dens = np.real(np.diagonal(P[0])).copy()
+    E = energies(s, T, LR, P, dens)
+    Etot = E.total(s)
+    V = potential(s, LR, dens)
+    dens_in = dens.copy()
+    P_in = P.copy()
+    logs = []
+    history = []
+    itmax = s.itmax if itmax is None else itmax
+    it = 0
+    last = {}
+    while it < itmax:
+        it += 1
+        sol = solve(s, g, T, V, P)
+        se, _, moms, sv, _, _ = sort_energies_1spin(s, g, sol["bands"], sol["evecs"])
+        nF, EF, nocc, npart, degf = fermi_level(s, se)
+        Pw = get_fock(s, g, sv, moms, nocc, npart, degf)
+        P_new = (Pw + sol["bulk"]) / complex(float(s.Nk), 0.0)
+        E_in, Etot_in = E, Etot
+        dens_new = np.real(np.diagonal(P_new[0])).copy()
+        step, E, t1, t2 = optimal_step(s, T, LR, P_new, P_in, dens_new, dens_in, E_in)
+        Etot = E.total(s)
+        P = step * P_new + (1.0 - step) * P_in
+        dens = np.real(np.diagonal(P[0])).copy()
+        dn = float(np.max(np.abs(dens - dens_in)))
+        V_old = V
+        V = potential(s, LR, dens)
+        res = hf_residual(s, T, V, V_old, P, P_in)
+        dens_in = dens.copy()
+        P_in = P.copy()
+        logs.append(IterationLog(it, dn, step, Etot_in - Etot, Etot_in, E_in.kinetic, E_in.fock,
+                                 E_in.hartree, E_in.hubbard, EF, nocc, npart, res))
+        last = dict(bands=sol["bands"], eigs=sol["eigs"], EF=EF, nocc=nocc, npart=npart, degf=degf,
+                    P_new=P_new, step=step, E1=t1, Ehalf=t2)
+        if keep_history:
+            history.append(dict(P=P.copy(), V=V.copy(), **last))
+        if residual_tol is not None and res < residual_tol:
+            break
+    return dict(P=P, V=V, dens=dens, E=E, Etot=Etot, logs=logs, geometry=g, tables=T, LR=LR,
+                history=history, **last)
+
+
+def order_parameters(s: Setup, g: Geometry, P) -> dict:
+    """Order parameters from P(R=0) and the site maps (Geometry.f90:1140-1223).
+
+    layer polarisation: sum over layer l of (l - (L-1)/2) * sum_i (n_i - 1/2);
+    sublattice polarisation: A-block minus B-block density;
+    C2T / C3 breaking norms: ||P(0) - g.P(0)||_F with g the site maps.
+    """
+    N = s.ndim
+    L = s.nlayers
+    per = N // L
+    n = np.real(np.diagonal(P[0])) - 0.5
+    layer = sum((l - (L - 1) / 2.0) * np.sum(n[l * per:(l + 1) * per]) for l in range(L))
+    sub = sum(np.sum(n[l * per:l * per + per // 2]) - np.sum(n[l * per + per // 2:(l + 1) * per]) for l in range(L))
+    c2 = g.c2pairs - 1
+    c3 = g.c3pairs - 1
+    P0 = P[0]
+    c2t = float(np.linalg.norm(P0 - P0[np.ix_(c2, c2)].T)) if np.all(c2 >= 0) else float("nan")
+    c3n = float(np.linalg.norm(P0 - P0[np.ix_(c3, c3)])) if np.all(c3 >= 0) else float("nan")
+    return dict(layer_polarization=float(layer), sublattice_polarization=float(sub), c2t_breaking=c2t,
+                c3_breaking=c3n)
