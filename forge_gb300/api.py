@@ -1,0 +1,385 @@
+"""ctypes binding of the C-ABI (include/forge_gpu.h, include/forge_host.h).
+
+The names mirror the reference's Fortran routines (Solve, SortEnergies_1Spin,
+GetFock, GetKineticEnergy, ..., OptimalStep) with the same argument meaning;
+arrays are numpy arrays in the reference's column-major layout.  There is no
+CPU fallback: every call goes through ``libforge_gpu.so`` and raises
+``ForgeError`` when the library or a CUDA device is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libforge_gpu.so")
+
+FORGE_PREC_FP64 = 0
+FORGE_PREC_MIXED = 1
+FORGE_DEG_REFERENCE = 0
+FORGE_DEG_CORRECTED = 1
+
+
+class ForgeError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"forge_gpu error {code}: {msg}")
+        self.code = code
+
+
+class forge_setup(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in (
+        "nlayers", "ntheta", "numk", "numS", "numI", "numC", "nscreen", "fphase", "ndim", "numb", "nLower", "nUpper",
+        "NeutralityPoint", "numNeighborCells", "degfactor_mode", "precision")] + [(n, C.c_double) for n in (
+            "nfilling", "U", "epsilon", "Delta", "xi", "alpha", "alphaH", "a0", "r0", "d0", "tz", "EnergyTolerance",
+            "StepAlternative")]
+
+
+class forge_iter_report(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "Step", "DensityConvergence", "TotalEnergyIn", "TotalEnergy", "KineticEnergyIn", "FockEnergyIn",
+        "HartreeEnergyIn", "HubbardEnergyIn", "KineticEnergy", "FockEnergy", "HartreeEnergy", "HubbardEnergy",
+        "FermiEnergy", "DegFactor", "residual")] + [(n, C.c_int64) for n in (
+            "nFermiLevel", "nOccStates", "nPartOccStates", "info")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class forge_scf_options(C.Structure):
+    _fields_ = [("itmax", C.c_int64), ("residual_tol", C.c_double), ("mixed_until", C.c_int64),
+                ("mixed_switch_tol", C.c_double), ("output_dir", C.c_char_p), ("statename", C.c_char_p)]
+
+
+class forge_scf_result(C.Structure):
+    _fields_ = [("iterations", C.c_int64), ("converged", C.c_int64), ("TotalEnergy", C.c_double),
+                ("Energies", C.c_double * 4), ("residual", C.c_double), ("seconds", C.c_double),
+                ("guess_seconds", C.c_double)]
+
+
+# exported entry points: name -> argtypes (all return int)
+_P = C.c_void_p
+_I = C.c_int64
+_D = C.c_double
+SIGNATURES = {
+    "forge_gpu_version": [],
+    "forge_gpu_init": [_P, _P, _P, _P, _P, _P, _P, _P],
+    "forge_gpu_finalize": [_P],
+    "forge_gpu_long_range": [_P, _P],
+    "forge_gpu_set_state": [_P, _P],
+    "forge_gpu_get_state": [_P, _P, _P, _P],
+    "forge_gpu_hamiltonian": [_P, _P, _P, _I, _I, _P],
+    "forge_gpu_zheevr_batch": [_P, _I, _P, _I, _P, _P],
+    "forge_gpu_solve": [_P, _P, _P, _P, _P, _P],
+    "forge_gpu_sort_energies": [_P, _P, _P, _P],
+    "forge_gpu_fermi": [_P, _D, _P, _P, _P, _P, _P],
+    "forge_gpu_get_fock": [_P, _D, _I, _I, _P],
+    "forge_gpu_energies": [_P, _P, _P, _P, _P, _P],
+    "forge_gpu_optimal_step": [_P, _P, _P],
+    "forge_gpu_mix_potential": [_P, _D, _P, _P],
+    "forge_gpu_plain_guess": [_P, _P],
+    "forge_gpu_prepare_state": [_P, _P],
+    "forge_gpu_scf_iteration": [_P, _P, _P],
+    "forge_gpu_set_precision": [_P, _I],
+    "forge_gpu_get_setup": [_P, _P],
+    "forge_gpu_synchronize": [_P],
+    "forge_host_setup": [_P],
+    "forge_host_geometry": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "forge_host_run_scf": [_P, _P, _P, _P, _P],
+    "forge_host_parameters_string": [_P, C.c_char_p, C.c_char_p, _I],
+}
+
+_LIB = None
+
+
+def load_library(path: Optional[str] = None):
+    """Loads libforge_gpu.so (raises ForgeError if it is not built)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ForgeError(-1, f"{p} is not built (run forge_gb300.build.build())")
+    lib = C.CDLL(p)
+    for name, argt in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.argtypes = argt
+        f.restype = C.c_int
+    lib.forge_gpu_last_error.restype = C.c_char_p
+    lib.forge_gpu_last_error.argtypes = []
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def _check(rc: int, allow_info: bool = False) -> int:
+    if rc < 0 or (rc > 0 and not allow_info):
+        msg = load_library().forge_gpu_last_error().decode(errors="replace")
+        raise ForgeError(rc, msg)
+    return rc
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f(a, dtype) -> np.ndarray:
+    """Fortran-ordered contiguous copy (or view) of a."""
+    return np.asfortranarray(np.asarray(a, dtype=dtype))
+
+
+# ---------------------------------------------------------------------------
+# Setup and geometry (host side, Setup.f90 / Geometry.f90 / Main.f90:102-163)
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class Setup:
+    """Runtime mirror of Setup.f90's parameters (names as in the reference)."""
+
+    ntheta: int = 9
+    nlayers: int = 2
+    RotateLayers: Sequence[int] = (-1, 1)
+    numk: int = 6
+    nfilling: float = 0.0
+    U: float = 4.0
+    epsilon: float = 10.0
+    Delta: float = 0.0
+    numI: int = 1
+    numC: int = 3
+    nscreen: int = 2
+    xi: float = 10.0 / 0.246
+    fphase: int = 0
+    numS: int = 1
+    EnergyTolerance: float = 0.0001
+    StepAlternative: float = 1.0
+    degfactor_mode: str = "reference"
+    precision: str = "fp64"
+
+    def to_struct(self) -> forge_setup:
+        s = forge_setup()
+        s.nlayers, s.ntheta, s.numk, s.numS = self.nlayers, self.ntheta, self.numk, self.numS
+        s.numI, s.numC, s.nscreen, s.fphase = self.numI, self.numC, self.nscreen, self.fphase
+        s.degfactor_mode = FORGE_DEG_REFERENCE if self.degfactor_mode == "reference" else FORGE_DEG_CORRECTED
+        s.precision = FORGE_PREC_MIXED if self.precision == "mixed" else FORGE_PREC_FP64
+        s.nfilling, s.U, s.epsilon, s.Delta, s.xi = self.nfilling, self.U, self.epsilon, self.Delta, self.xi
+        s.EnergyTolerance, s.StepAlternative = self.EnergyTolerance, self.StepAlternative
+        _check(load_library().forge_host_setup(C.byref(s)))
+        return s
+
+
+@dataclasses.dataclass
+class Geometry:
+    Coords: np.ndarray            # (ndim, 3)
+    nUnitCell_1: np.ndarray
+    nUnitCell_2: np.ndarray
+    tn: np.ndarray                # (2, 3): t1, t2, t3
+    g1: np.ndarray
+    g12: np.ndarray
+    MomentaValues: np.ndarray     # (numk, numk, 2)
+    nMomentaComponents: np.ndarray  # (Nk, 2)
+    nMomentaFlattened: np.ndarray   # (numk, numk)
+    nC2pairs: np.ndarray
+    nC3pairs: np.ndarray
+    c2_count: int
+    c3_count: int
+
+
+def build_geometry(setup: Setup) -> Geometry:
+    """Main.f90:102-163 through forge_host_geometry."""
+    s = setup.to_struct()
+    N, numk = s.ndim, s.numk
+    Nk = numk * numk
+    out = Geometry(
+        Coords=np.zeros((N, 3), order="F"), nUnitCell_1=np.zeros(4, np.int64), nUnitCell_2=np.zeros(4, np.int64),
+        tn=np.zeros((2, 3), order="F"), g1=np.zeros(2), g12=np.zeros(2), MomentaValues=np.zeros((numk, numk, 2), order="F"),
+        nMomentaComponents=np.zeros((Nk, 2), np.int64, order="F"),
+        nMomentaFlattened=np.zeros((numk, numk), np.int64, order="F"), nC2pairs=np.zeros(N, np.int64),
+        nC3pairs=np.zeros(N, np.int64), c2_count=0, c3_count=0)
+    rl = np.ascontiguousarray(setup.RotateLayers, dtype=np.int64)
+    counts = np.zeros(2, np.int64)
+    _check(load_library().forge_host_geometry(
+        C.byref(s), _ptr(rl), _ptr(out.Coords), _ptr(out.nUnitCell_1), _ptr(out.nUnitCell_2), _ptr(out.tn),
+        _ptr(out.g1), _ptr(out.g12), _ptr(out.MomentaValues), _ptr(out.nMomentaComponents),
+        _ptr(out.nMomentaFlattened), _ptr(out.nC2pairs), _ptr(out.nC3pairs), _ptr(counts)))
+    out.c2_count, out.c3_count = int(counts[0]), int(counts[1])
+    return out
+
+
+def parameters_string(setup: Setup, statename: str = "SSS") -> str:
+    s = setup.to_struct()
+    buf = C.create_string_buffer(256)
+    _check(load_library().forge_host_parameters_string(C.byref(s), statename.encode(), buf, 256))
+    return buf.value.decode()
+
+
+# ---------------------------------------------------------------------------
+# Device context: the reference's Hartree-Fock routines
+# ---------------------------------------------------------------------------
+class HartreeFock:
+    """One device context; methods mirror HartreeFock.f90 / LapackRoutines.f90 routines."""
+
+    def __init__(self, setup: Setup, geometry: Optional[Geometry] = None):
+        self.setup = setup
+        self.s = setup.to_struct()
+        self.geometry = geometry if geometry is not None else build_geometry(setup)
+        g = self.geometry
+        self.N = self.s.ndim
+        self.Nk = self.s.numk ** 2
+        self.numb = self.s.numb
+        self._keep = [_f(g.Coords, np.float64), _f(g.nUnitCell_1, np.int64), _f(g.nUnitCell_2, np.int64),
+                      _f(g.tn, np.float64), _f(g.MomentaValues, np.float64), _f(g.nMomentaComponents, np.int64)]
+        ctx = C.c_void_p()
+        lib = load_library()
+        _check(lib.forge_gpu_init(C.byref(self.s), *[_ptr(a) for a in self._keep], C.byref(ctx)))
+        self.ctx = ctx
+        self.lib = lib
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.forge_gpu_finalize(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- shapes
+    def _zfock_shape(self):
+        return (self.N, self.N, 4)
+
+    def set_precision(self, precision: str):
+        _check(self.lib.forge_gpu_set_precision(self.ctx, FORGE_PREC_MIXED if precision == "mixed" else FORGE_PREC_FP64))
+
+    def LongRangeInteraction(self, copy_out: bool = True) -> Optional[np.ndarray]:
+        """HartreeFock.f90:14-53."""
+        LR = np.zeros((self.N, self.N), order="F") if copy_out else None
+        _check(self.lib.forge_gpu_long_range(self.ctx, _ptr(LR)))
+        return LR
+
+    def HamiltonianHartreeFock(self, Potential, zFock, k0: int = 0, nk: int = 1) -> np.ndarray:
+        """Lower triangles of H(k) for flat k indices k0..k0+nk-1 (HartreeFock.f90:57-127)."""
+        V = None if Potential is None else _f(Potential, np.float64)
+        P = None if zFock is None else _f(zFock, np.complex128)
+        H = np.zeros((self.N, self.N, nk), dtype=np.complex128, order="F")
+        _check(self.lib.forge_gpu_hamiltonian(self.ctx, _ptr(V), _ptr(P), k0, nk, _ptr(H)))
+        return H
+
+    def zheevr_batch(self, A: np.ndarray, iu: int, vectors: bool = True):
+        """zdiagRed (LapackRoutines.f90:381-433) on a batch A[:, :, b] (lower triangles)."""
+        A = _f(A, np.complex128)
+        if A.ndim == 2:
+            A = A[:, :, None]
+        nb = A.shape[2]
+        w = np.zeros((iu, nb), order="F")
+        Z = np.zeros((self.N, iu, nb), dtype=np.complex128, order="F") if vectors else None
+        info = _check(self.lib.forge_gpu_zheevr_batch(self.ctx, nb, _ptr(A), iu, _ptr(w), _ptr(Z)), allow_info=True)
+        return w, Z, info
+
+    def Solve(self, Potential=None, zFock=None, bands=True, vectors=False, bulk=False):
+        """Solve (HartreeFock.f90:402-483): returns (Bands, zEigenvectors, zFockBulk, info)."""
+        V = None if Potential is None else _f(Potential, np.float64)
+        P = None if zFock is None else _f(zFock, np.complex128)
+        B = np.zeros((self.numb, self.Nk), order="F") if bands else None
+        E = np.zeros((self.N, self.numb, self.Nk), dtype=np.complex128, order="F") if vectors else None
+        FB = np.zeros(self._zfock_shape(), dtype=np.complex128, order="F") if bulk else None
+        info = _check(self.lib.forge_gpu_solve(self.ctx, _ptr(V), _ptr(P), _ptr(B), _ptr(E), _ptr(FB)),
+                      allow_info=True)
+        return B, E, FB, info
+
+    def SortEnergies_1Spin(self):
+        """HartreeFock.f90:885-925: (SortedEnergies, nSortedMomenta, sorted flat icount)."""
+        n = self.numb * self.Nk
+        e = np.zeros(n)
+        m = np.zeros((n, 2), np.int64, order="F")
+        idx = np.zeros(n, np.int64)
+        _check(self.lib.forge_gpu_sort_energies(self.ctx, _ptr(e), _ptr(m), _ptr(idx)))
+        return e, m, idx
+
+    def FermiLevel(self, nfilling: Optional[float] = None):
+        """Main.f90:400-412: (nFermiLevel, FermiEnergy, nOccStates, nPartOccStates, DegFactor)."""
+        nf, no, npart = C.c_int64(), C.c_int64(), C.c_int64()
+        ef, deg = C.c_double(), C.c_double()
+        nfill = self.setup.nfilling if nfilling is None else nfilling
+        _check(self.lib.forge_gpu_fermi(self.ctx, nfill, C.byref(nf), C.byref(ef), C.byref(no), C.byref(npart),
+                                        C.byref(deg)))
+        return nf.value, ef.value, no.value, npart.value, deg.value
+
+    def GetFock(self, DegFactor: float, nOccStates: int, nPartOccStates: int, copy_out: bool = True):
+        """GetFock + Main.f90:510-511: P_new = (window + zFockBulk)/Nk."""
+        P = np.zeros(self._zfock_shape(), dtype=np.complex128, order="F") if copy_out else None
+        _check(self.lib.forge_gpu_get_fock(self.ctx, DegFactor, nOccStates, nPartOccStates, _ptr(P)))
+        return P
+
+    def Energies(self, zFock=None):
+        """GetKineticEnergy, GetFockEnergy, GetHartreeHubbardEnergy: (Kinetic, Fock, Hartree, Hubbard)."""
+        P = None if zFock is None else _f(zFock, np.complex128)
+        out = [C.c_double() for _ in range(4)]
+        _check(self.lib.forge_gpu_energies(self.ctx, _ptr(P), *[C.byref(o) for o in out]))
+        return tuple(o.value for o in out)
+
+    def OptimalStep(self, energies_in: Sequence[float]):
+        """OptimalStep (HartreeFock.f90:1148-1227) on the device (P_new, P_in): (Step, energies)."""
+        E = np.ascontiguousarray(energies_in, dtype=np.float64).copy()
+        step = C.c_double()
+        _check(self.lib.forge_gpu_optimal_step(self.ctx, C.byref(step), _ptr(E)))
+        return step.value, tuple(E)
+
+    def MixPotential(self, Step: float):
+        """Main.f90:558-595: returns (DensityConvergence, residual)."""
+        dn, res = C.c_double(), C.c_double()
+        _check(self.lib.forge_gpu_mix_potential(self.ctx, Step, C.byref(dn), C.byref(res)))
+        return dn.value, res.value
+
+    def PlainGuess(self):
+        E = np.zeros(4)
+        info = _check(self.lib.forge_gpu_plain_guess(self.ctx, _ptr(E)), allow_info=True)
+        return tuple(E), info
+
+    def SetState(self, zFock):
+        P = _f(zFock, np.complex128)
+        _check(self.lib.forge_gpu_set_state(self.ctx, _ptr(P)))
+
+    def PrepareState(self):
+        E = np.zeros(4)
+        _check(self.lib.forge_gpu_prepare_state(self.ctx, _ptr(E)))
+        return tuple(E)
+
+    def GetState(self):
+        P = np.zeros(self._zfock_shape(), dtype=np.complex128, order="F")
+        d = np.zeros(self.N)
+        V = np.zeros(self.N)
+        _check(self.lib.forge_gpu_get_state(self.ctx, _ptr(P), _ptr(d), _ptr(V)))
+        return P, d, V
+
+    def ScfIteration(self, energies: Optional[Sequence[float]] = None):
+        E = None if energies is None else np.ascontiguousarray(energies, dtype=np.float64).copy()
+        rep = forge_iter_report()
+        info = _check(self.lib.forge_gpu_scf_iteration(self.ctx, _ptr(E), C.byref(rep)), allow_info=True)
+        return rep.as_dict(), (None if E is None else tuple(E)), info
+
+    def RunScf(self, itmax: int, residual_tol: float = 0.0, mixed_until: int = 0, mixed_switch_tol: float = 0.0,
+               zFock_init=None, output_dir: Optional[str] = None, statename: str = "SSS"):
+        """Main.f90:236-679 via forge_host_run_scf: (result dict, list of per-iteration reports)."""
+        opts = forge_scf_options(itmax, residual_tol, mixed_until, mixed_switch_tol,
+                                 None if output_dir is None else output_dir.encode(), statename.encode())
+        res = forge_scf_result()
+        reps = (forge_iter_report * max(1, itmax))()
+        P0 = None if zFock_init is None else _f(zFock_init, np.complex128)
+        _check(self.lib.forge_host_run_scf(self.ctx, C.byref(opts), _ptr(P0), C.byref(res), reps))
+        out = dict(iterations=res.iterations, converged=bool(res.converged), TotalEnergy=res.TotalEnergy,
+                   Energies=tuple(res.Energies), residual=res.residual, seconds=res.seconds,
+                   guess_seconds=res.guess_seconds)
+        return out, [reps[i].as_dict() for i in range(res.iterations)]
+
+    def synchronize(self):
+        _check(self.lib.forge_gpu_synchronize(self.ctx))

@@ -1,0 +1,778 @@
+// C-ABI entry points (include/forge_gpu.h): one per reference routine of the SCF
+// path, plus a fused device-resident iteration.  Host code here is compiled with
+// -ffp-contract=off so that the k.R phases follow the reference's unfused dot product.
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <mutex>
+
+#include "eig.cuh"
+#include "proj.cuh"
+
+namespace forge {
+
+static thread_local std::string g_err;
+static thread_local int g_errcode = 0;
+
+void set_error(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    g_errcode = code;
+}
+int last_error_code() { return g_errcode; }
+
+int DevBuf::ensure(size_t nbytes) {
+    if (nbytes <= bytes && ptr) return 0;
+    release();
+    if (nbytes == 0) return 0;
+    cudaError_t e = cudaMalloc(&ptr, nbytes);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        bytes = 0;
+        set_error(FORGE_ERR_NOMEM, "cudaMalloc(%zu) failed: %s", nbytes, cudaGetErrorString(e));
+        return FORGE_ERR_NOMEM;
+    }
+    bytes = nbytes;
+    return 0;
+}
+void DevBuf::release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+// defined in scf.cu
+int build_energy_tables(Context& c, DevBuf& te);
+int launch_sort_fermi(Context& c, const double* w, double nfilling, double* sorted_e, int64_t* sorted_idx,
+                      WinState* states, ScfScalars* sc);
+int scf_energy_forms(Context& c, const double* te, const double2* Pa, const double2* Pb, const double* da,
+                     const double* db, double* y, double* work, ScfScalars* sc);
+size_t scf_work_doubles(int64_t N);
+int scf_oda(Context& c, ScfScalars* sc, int mode);
+int scf_mix(Context& c, double2* P, const double2* Pn, double* dens, double* V, const double* y, double* work,
+            ScfScalars* sc);
+int scf_combine(Context& c, double2* win, const double2* bulk);
+int scf_density(Context& c, const double2* P, double* dens);
+int scf_potential(Context& c, const double* y, const double* dens, double* V);
+// mixed-precision eigen-solver (eig_mixed.cu)
+int eig_mixed(cudaStream_t st, EigArgs& g, void* mixed_ws);
+size_t eig_mixed_workspace_bytes(int64_t n, int64_t iu, int64_t batch);
+
+}  // namespace forge
+
+using namespace forge;
+
+struct forge_ctx {
+    Context c;
+    DevBuf te;           // energy tables
+    DevBuf Pn, win;      // P_new, window accumulator / scratch
+    DevBuf eigws, mixws; // eigen-solver workspaces
+    DevBuf states, sorted_e, sorted_idx, sc, work, y, dens_new, w;
+    int64_t eig_batch = 0;
+    bool have_solve = false, have_sort = false, have_pnew = false, have_state = false;
+    std::vector<int64_t> h_sorted_idx;
+};
+
+namespace {
+
+int check_ctx(forge_ctx* x) {
+    if (!x) {
+        set_error(FORGE_ERR_ARG, "null context");
+        return FORGE_ERR_ARG;
+    }
+    return 0;
+}
+
+int choose_batch(forge_ctx* x) {
+    Context& c = x->c;
+    const int64_t N = c.N, iu = c.nUpper;
+    size_t per_k = (size_t)N * N * 16 + eig_workspace_bytes(N, iu, 1);
+    if (c.precision == FORGE_PREC_MIXED) per_k += eig_mixed_workspace_bytes(N, iu, 1);
+    size_t freeb = 0, totalb = 0;
+    cudaMemGetInfo(&freeb, &totalb);
+    size_t budget = freeb > (size_t)8 << 30 ? (freeb - ((size_t)8 << 30)) / 2 : freeb / 4;
+    int64_t b = (int64_t)(budget / per_k);
+    if (b < 1) b = 1;
+    if (b > c.Nk) b = c.Nk;
+    return (int)b;
+}
+
+int ensure_solve_buffers(forge_ctx* x) {
+    Context& c = x->c;
+    const int64_t N = c.N, iu = c.nUpper, Nk = c.Nk;
+    const size_t NN = (size_t)N * N;
+    if (x->eig_batch == 0) x->eig_batch = choose_batch(x);
+    const int64_t B = x->eig_batch;
+    FORGE_TRY(c.H.ensure((size_t)B * NN * sizeof(double2)));
+    FORGE_TRY(c.X.ensure((size_t)Nk * N * iu * sizeof(double2)));
+    FORGE_TRY(x->w.ensure((size_t)Nk * iu * sizeof(double)));
+    FORGE_TRY(x->eigws.ensure(eig_workspace_bytes(N, iu, B)));
+    if (c.precision == FORGE_PREC_MIXED) FORGE_TRY(x->mixws.ensure(eig_mixed_workspace_bytes(N, iu, B)));
+    FORGE_TRY(c.bulk.ensure(4 * NN * sizeof(double2)));
+    return 0;
+}
+
+int upload_state(forge_ctx* x, const double* Potential, const double* zFock) {
+    Context& c = x->c;
+    const size_t NN = (size_t)c.N * c.N;
+    if (Potential) FORGE_CUDA(cudaMemcpyAsync(c.V.ptr, Potential, c.N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    if (zFock) {
+        FORGE_CUDA(cudaMemcpyAsync(c.P.ptr, zFock, 4 * NN * sizeof(double2), cudaMemcpyHostToDevice, c.stream));
+        x->have_state = true;
+    }
+    return 0;
+}
+
+// eigen-solve of the batch of H already assembled in c.H for k in [k0, k0+nb)
+int eig_batch_run(forge_ctx* x, int64_t k0, int64_t nb, int* info) {
+    Context& c = x->c;
+    const int64_t N = c.N, iu = c.nUpper;
+    EigArgs g{};
+    g.n = N;
+    g.iu = iu;
+    g.batch = nb;
+    g.A = c.H.as<double2>();
+    g.lda = N;
+    g.strideA = N * N;
+    g.X = c.X.as<double2>() + (size_t)k0 * N * iu;
+    g.ldx = N;
+    g.strideX = N * iu;
+    g.w = x->w.as<double>() + (size_t)k0 * iu;
+    g.ortol_rel = 1e-7;
+    eig_bind_workspace(g, x->eigws.ptr);
+    if (c.precision == FORGE_PREC_MIXED) {
+        FORGE_TRY(eig_mixed(c.stream, g, x->mixws.ptr));
+    } else {
+        FORGE_TRY(eig_fp64(c.stream, g));
+    }
+    std::vector<int> fails(nb);
+    FORGE_CUDA(cudaMemcpyAsync(fails.data(), g.fail, nb * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    int bad = 0;
+    for (int64_t b = 0; b < nb; ++b) bad += fails[b] ? 1 : 0;
+    *info += bad;
+    return 0;
+}
+
+// full Solve on the device: H(k), eigenpairs, bulk projector (not divided by Nk)
+int solve_device(forge_ctx* x, int* info) {
+    Context& c = x->c;
+    FORGE_TRY(ensure_solve_buffers(x));
+    const int64_t N = c.N, iu = c.nUpper, Nk = c.Nk, B = x->eig_batch;
+    const size_t NN = (size_t)N * N;
+    FORGE_CUDA(cudaMemsetAsync(c.bulk.ptr, 0, 4 * NN * sizeof(double2), c.stream));
+    *info = 0;
+    std::vector<double2> bph(Nk * 4);
+    FORGE_CUDA(cudaMemcpyAsync(bph.data(), c.bphase.ptr, Nk * 4 * sizeof(double2), cudaMemcpyDeviceToHost, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    for (int64_t k0 = 0; k0 < Nk; k0 += B) {
+        const int64_t nb = (Nk - k0 < B) ? Nk - k0 : B;
+        FORGE_TRY(launch_assemble(c, c.V.as<double>(), c.P.as<double2>(), k0, nb, c.H.as<double2>()));
+        FORGE_TRY(eig_batch_run(x, k0, nb, info));
+        for (int64_t k = k0; k < k0 + nb; ++k) {
+            const double2* Xk = c.X.as<double2>() + (size_t)k * N * iu;
+            FORGE_TRY(bulk_projector_fp64(c.stream, Xk, N, N, c.nLower - 1, &bph[k * 4], c.bulk.as<double2>()));
+        }
+    }
+    x->have_solve = true;
+    x->have_sort = false;
+    return 0;
+}
+
+int sort_device(forge_ctx* x, double nfilling) {
+    Context& c = x->c;
+    if (!x->have_solve) {
+        set_error(FORGE_ERR_STATE, "sort before solve");
+        return FORGE_ERR_STATE;
+    }
+    const int64_t nw = c.numb * c.Nk;
+    FORGE_TRY(x->sorted_e.ensure(nw * sizeof(double)));
+    FORGE_TRY(x->sorted_idx.ensure(nw * sizeof(int64_t)));
+    FORGE_TRY(x->states.ensure(nw * sizeof(WinState)));
+    FORGE_TRY(launch_sort_fermi(c, x->w.as<double>(), nfilling, x->sorted_e.as<double>(), x->sorted_idx.as<int64_t>(),
+                                x->states.as<WinState>(), x->sc.as<ScfScalars>()));
+    x->have_sort = true;
+    return 0;
+}
+
+int get_fock_device(forge_ctx* x, int64_t nstates) {
+    Context& c = x->c;
+    const size_t NN = (size_t)c.N * c.N;
+    FORGE_TRY(x->Pn.ensure(4 * NN * sizeof(double2)));
+    FORGE_CUDA(cudaMemsetAsync(x->Pn.ptr, 0, 4 * NN * sizeof(double2), c.stream));
+    FORGE_TRY(window_projector_fp64(c.stream, x->states.as<WinState>(), nstates, c.X.as<double2>(), c.N,
+                                    c.N * c.nUpper, c.N, x->Pn.as<double2>()));
+    FORGE_TRY(scf_combine(c, x->Pn.as<double2>(), c.bulk.as<double2>()));
+    x->have_pnew = true;
+    return 0;
+}
+
+int read_scalars(forge_ctx* x, ScfScalars* h) {
+    Context& c = x->c;
+    FORGE_CUDA(cudaMemcpyAsync(h, x->sc.ptr, sizeof(ScfScalars), cudaMemcpyDeviceToHost, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+int write_scalars(forge_ctx* x, const ScfScalars* h) {
+    Context& c = x->c;
+    FORGE_CUDA(cudaMemcpyAsync(x->sc.ptr, h, sizeof(ScfScalars), cudaMemcpyHostToDevice, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+// energies and potential of the current state P (Main.f90:290-346)
+int prepare_state_device(forge_ctx* x, double* Energies) {
+    Context& c = x->c;
+    FORGE_TRY(scf_density(c, c.P.as<double2>(), c.dens.as<double>()));
+    FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), c.P.as<double2>(), c.dens.as<double>(),
+                               c.dens.as<double>(), x->y.as<double>(), x->work.as<double>(), x->sc.as<ScfScalars>()));
+    FORGE_TRY(scf_oda(c, x->sc.as<ScfScalars>(), 1));
+    FORGE_TRY(scf_potential(c, x->y.as<double>(), c.dens.as<double>(), c.V.as<double>()));
+    ScfScalars h;
+    FORGE_TRY(read_scalars(x, &h));
+    for (int t = 0; t < 4; ++t) h.Ein[t] = h.Eout[t];
+    FORGE_TRY(write_scalars(x, &h));
+    if (Energies)
+        for (int t = 0; t < 4; ++t) Energies[t] = h.Eout[t];
+    x->have_state = true;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* forge_gpu_last_error(void) { return g_err.c_str(); }
+int forge_gpu_version(void) { return 1; }
+
+int forge_gpu_init(const forge_setup* s, const double* Coords, const int64_t* nUnitCell_1, const int64_t* nUnitCell_2,
+                   const double* tn, const double* MomentaValues, const int64_t* nMomentaComponents,
+                   forge_ctx** out) {
+    if (!s || !Coords || !nUnitCell_1 || !nUnitCell_2 || !tn || !MomentaValues || !nMomentaComponents || !out) {
+        set_error(FORGE_ERR_ARG, "forge_gpu_init: null argument");
+        return FORGE_ERR_ARG;
+    }
+    *out = nullptr;
+    if (s->numS != 1) {
+        set_error(FORGE_ERR_ARG, "numS=%lld is not supported (only numS=1)", (long long)s->numS);
+        return FORGE_ERR_ARG;
+    }
+    if (s->numNeighborCells != 4) {
+        set_error(FORGE_ERR_ARG, "numNeighborCells=%lld is not supported (numI=1 gives 4)",
+                  (long long)s->numNeighborCells);
+        return FORGE_ERR_ARG;
+    }
+    const int64_t nexp = s->nlayers * 2 * (s->ntheta * s->ntheta + (s->ntheta + 1) * (s->ntheta + 1) +
+                                           (s->ntheta + 1) * s->ntheta);
+    if (s->ndim != nexp || s->ndim < 2 || s->numk < 1 || s->nUpper > s->ndim || s->nLower < 1 ||
+        s->nUpper - s->nLower + 1 != s->numb) {
+        set_error(FORGE_ERR_ARG, "inconsistent setup (ndim=%lld expected %lld, nLower=%lld nUpper=%lld numb=%lld)",
+                  (long long)s->ndim, (long long)nexp, (long long)s->nLower, (long long)s->nUpper,
+                  (long long)s->numb);
+        return FORGE_ERR_ARG;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        set_error(FORGE_ERR_CUDA, "no CUDA device");
+        return FORGE_ERR_CUDA;
+    }
+    forge_ctx* x = new forge_ctx();
+    Context& c = x->c;
+    c.s = *s;
+    c.N = s->ndim;
+    c.Nk = s->numk * s->numk;
+    c.nnc = 4;
+    c.nLower = s->nLower;
+    c.nUpper = s->nUpper;
+    c.numb = s->numb;
+    c.NP = s->NeutralityPoint;
+    c.precision = (int)s->precision;
+    c.t1[0] = tn[0];
+    c.t1[1] = tn[1];
+    c.t2[0] = tn[2];
+    c.t2[1] = tn[3];
+    c.ucell1.assign(nUnitCell_1, nUnitCell_1 + 4);
+    c.ucell2.assign(nUnitCell_2, nUnitCell_2 + 4);
+    c.kcomp.assign(nMomentaComponents, nMomentaComponents + 2 * c.Nk);
+    c.kvals.assign(MomentaValues, MomentaValues + 2 * s->numk * s->numk);
+    c.coords_h.assign(Coords, Coords + 3 * c.N);
+    int rc = 0;
+    auto fail = [&](int r) {
+        forge_gpu_finalize(x);
+        return r;
+    };
+    if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error(FORGE_ERR_CUDA, "stream creation failed");
+        delete x;
+        return FORGE_ERR_CUDA;
+    }
+    const int64_t N = c.N, Nk = c.Nk, numk = s->numk;
+    // phases: exp(-i k.R_c) with the floating-point dot (HartreeFock.f90:90) and the integer
+    // Bloch phase exp(-2 pi i (ivk1 n1 + ivk2 n1 + ivk2 n2)/numk) (HartreeFock.f90:471)
+    std::vector<double2> kph(Nk * 3), bph(Nk * 4);
+    std::vector<double> kvec(Nk * 2);
+    const double pi = 4.0 * std::atan(1.0);
+    for (int64_t k = 0; k < Nk; ++k) {
+        const int64_t ivk1 = c.kcomp[k], ivk2 = c.kcomp[k + Nk];
+        const double vk0 = c.kvals[ivk1 + ivk2 * numk], vk1 = c.kvals[ivk1 + ivk2 * numk + numk * numk];
+        kvec[2 * k] = vk0;
+        kvec[2 * k + 1] = vk1;
+        for (int q = 0; q < 4; ++q) {
+            const int64_t n1 = c.ucell1[q], n2 = c.ucell2[q];
+            if (q > 0) {
+                const double rx = (double)n1 * c.t1[0] + (double)n2 * c.t2[0];
+                const double ry = (double)n1 * c.t1[1] + (double)n2 * c.t2[1];
+                const double th = vk0 * rx + vk1 * ry;
+                kph[k * 3 + q - 1] = make_double2(std::cos(th), -std::sin(th));
+            }
+            const double ph = -(2.0 * pi * (double)(ivk1 * n1 + ivk2 * n1 + ivk2 * n2) / (double)numk);
+            bph[k * 4 + q] = (q == 0) ? make_double2(1.0, 0.0) : make_double2(std::cos(ph), std::sin(ph));
+        }
+    }
+    const size_t NN = (size_t)N * N;
+    if ((rc = c.coords.ensure(3 * N * sizeof(double))) || (rc = c.kphase.ensure(Nk * 3 * sizeof(double2))) ||
+        (rc = c.bphase.ensure(Nk * 4 * sizeof(double2))) || (rc = c.kvecs.ensure(Nk * 2 * sizeof(double))) ||
+        (rc = c.P.ensure(4 * NN * sizeof(double2))) || (rc = c.V.ensure(N * sizeof(double))) ||
+        (rc = c.dens.ensure(N * sizeof(double))) || (rc = x->dens_new.ensure(N * sizeof(double))) ||
+        (rc = x->sc.ensure(sizeof(ScfScalars))) || (rc = x->work.ensure(scf_work_doubles(N) * sizeof(double))) ||
+        (rc = x->y.ensure(2 * N * sizeof(double))))
+        return fail(rc);
+    if (cudaMemcpyAsync(c.coords.ptr, Coords, 3 * N * sizeof(double), cudaMemcpyHostToDevice, c.stream) ||
+        cudaMemcpyAsync(c.kphase.ptr, kph.data(), Nk * 3 * sizeof(double2), cudaMemcpyHostToDevice, c.stream) ||
+        cudaMemcpyAsync(c.bphase.ptr, bph.data(), Nk * 4 * sizeof(double2), cudaMemcpyHostToDevice, c.stream) ||
+        cudaMemcpyAsync(c.kvecs.ptr, kvec.data(), Nk * 2 * sizeof(double), cudaMemcpyHostToDevice, c.stream) ||
+        cudaMemsetAsync(c.P.ptr, 0, 4 * NN * sizeof(double2), c.stream) ||
+        cudaMemsetAsync(c.V.ptr, 0, N * sizeof(double), c.stream) ||
+        cudaMemsetAsync(x->sc.ptr, 0, sizeof(ScfScalars), c.stream)) {
+        set_error(FORGE_ERR_CUDA, "forge_gpu_init: upload failed");
+        return fail(FORGE_ERR_CUDA);
+    }
+    if ((rc = launch_pair_tables(c)) || (rc = build_energy_tables(c, x->te))) return fail(rc);
+    if (cudaStreamSynchronize(c.stream) != cudaSuccess) {
+        set_error(FORGE_ERR_CUDA, "forge_gpu_init: %s", cudaGetErrorString(cudaGetLastError()));
+        return fail(FORGE_ERR_CUDA);
+    }
+    *out = x;
+    return 0;
+}
+
+int forge_gpu_finalize(forge_ctx* x) {
+    if (!x) return 0;
+    Context& c = x->c;
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    DevBuf* bufs[] = {&c.coords, &c.tab_t, &c.tab_v, &c.LR, &c.P, &c.P_in, &c.P_new, &c.bulk, &c.V, &c.dens,
+                      &c.dens_in, &c.V_old, &c.H, &c.X, &c.bands, &c.evals, &c.kvecs, &c.kphase, &c.bphase,
+                      &c.sort_idx, &c.sort_e, &c.red, &c.scalars, &x->te, &x->Pn, &x->win, &x->eigws, &x->mixws,
+                      &x->states, &x->sorted_e, &x->sorted_idx, &x->sc, &x->work, &x->y, &x->dens_new, &x->w};
+    for (DevBuf* b : bufs) b->release();
+    if (c.stream) cudaStreamDestroy(c.stream);
+    delete x;
+    return 0;
+}
+
+int forge_gpu_set_precision(forge_ctx* x, int64_t precision) {
+    FORGE_TRY(check_ctx(x));
+    if (precision != FORGE_PREC_FP64 && precision != FORGE_PREC_MIXED) {
+        set_error(FORGE_ERR_ARG, "unknown precision %lld", (long long)precision);
+        return FORGE_ERR_ARG;
+    }
+    if (x->c.precision != (int)precision) {
+        x->c.precision = (int)precision;
+        x->eig_batch = 0;
+    }
+    return 0;
+}
+
+int forge_gpu_get_setup(forge_ctx* x, forge_setup* s) {
+    FORGE_TRY(check_ctx(x));
+    if (!s) {
+        set_error(FORGE_ERR_ARG, "forge_gpu_get_setup: null setup");
+        return FORGE_ERR_ARG;
+    }
+    *s = x->c.s;
+    s->precision = x->c.precision;
+    return 0;
+}
+
+int forge_gpu_synchronize(forge_ctx* x) {
+    FORGE_TRY(check_ctx(x));
+    FORGE_CUDA(cudaStreamSynchronize(x->c.stream));
+    return 0;
+}
+
+int forge_gpu_long_range(forge_ctx* x, double* LongRange) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    FORGE_TRY(launch_long_range(c));
+    if (LongRange)
+        FORGE_CUDA(cudaMemcpyAsync(LongRange, c.LR.ptr, (size_t)c.N * c.N * sizeof(double), cudaMemcpyDeviceToHost,
+                                   c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+int forge_gpu_set_state(forge_ctx* x, const double* zFock) {
+    FORGE_TRY(check_ctx(x));
+    if (!zFock) {
+        set_error(FORGE_ERR_ARG, "forge_gpu_set_state: null zFock");
+        return FORGE_ERR_ARG;
+    }
+    FORGE_TRY(upload_state(x, nullptr, zFock));
+    FORGE_CUDA(cudaStreamSynchronize(x->c.stream));
+    return 0;
+}
+
+int forge_gpu_get_state(forge_ctx* x, double* zFock, double* Density, double* Potential) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    const size_t NN = (size_t)c.N * c.N;
+    if (zFock)
+        FORGE_CUDA(cudaMemcpyAsync(zFock, c.P.ptr, 4 * NN * sizeof(double2), cudaMemcpyDeviceToHost, c.stream));
+    if (Density) {
+        FORGE_TRY(scf_density(c, c.P.as<double2>(), x->dens_new.as<double>()));
+        FORGE_CUDA(cudaMemcpyAsync(Density, x->dens_new.ptr, c.N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    }
+    if (Potential)
+        FORGE_CUDA(cudaMemcpyAsync(Potential, c.V.ptr, c.N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+int forge_gpu_hamiltonian(forge_ctx* x, const double* Potential, const double* zFock, int64_t k0, int64_t nk,
+                          double* H) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (k0 < 0 || nk < 1 || k0 + nk > c.Nk || !H) {
+        set_error(FORGE_ERR_ARG, "forge_gpu_hamiltonian: bad k range");
+        return FORGE_ERR_ARG;
+    }
+    FORGE_TRY(upload_state(x, Potential, zFock));
+    const size_t NN = (size_t)c.N * c.N;
+    DevBuf tmp;
+    FORGE_TRY(tmp.ensure(nk * NN * sizeof(double2)));
+    int rc = 0;
+    if (cudaMemsetAsync(tmp.ptr, 0, nk * NN * sizeof(double2), c.stream) != cudaSuccess) rc = FORGE_ERR_CUDA;
+    if (!rc) rc = launch_assemble(c, c.V.as<double>(), c.P.as<double2>(), k0, nk, tmp.as<double2>());
+    if (!rc && cudaMemcpyAsync(H, tmp.ptr, nk * NN * sizeof(double2), cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
+        rc = FORGE_ERR_CUDA;
+    if (!rc && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = FORGE_ERR_CUDA;
+    if (rc == FORGE_ERR_CUDA) set_error(rc, "forge_gpu_hamiltonian: %s", cudaGetErrorString(cudaGetLastError()));
+    tmp.release();
+    return rc;
+}
+
+int forge_gpu_zheevr_batch(forge_ctx* x, int64_t nb, const double* A, int64_t iu, double* w, double* Z) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    const int64_t N = c.N;
+    if (nb < 1 || iu < 1 || iu > N || !A || !w) {
+        set_error(FORGE_ERR_ARG, "forge_gpu_zheevr_batch: bad arguments");
+        return FORGE_ERR_ARG;
+    }
+    const size_t NN = (size_t)N * N;
+    DevBuf dA, dX, dw, ws, mws;
+    int rc = 0;
+    if ((rc = dA.ensure(nb * NN * sizeof(double2))) || (rc = dX.ensure(nb * N * iu * sizeof(double2))) ||
+        (rc = dw.ensure(nb * iu * sizeof(double))) || (rc = ws.ensure(eig_workspace_bytes(N, iu, nb))))
+        return rc;
+    if (c.precision == FORGE_PREC_MIXED && (rc = mws.ensure(eig_mixed_workspace_bytes(N, iu, nb)))) return rc;
+    FORGE_CUDA(cudaMemcpyAsync(dA.ptr, A, nb * NN * sizeof(double2), cudaMemcpyHostToDevice, c.stream));
+    EigArgs g{};
+    g.n = N;
+    g.iu = iu;
+    g.batch = nb;
+    g.A = dA.as<double2>();
+    g.lda = N;
+    g.strideA = N * N;
+    g.X = dX.as<double2>();
+    g.ldx = N;
+    g.strideX = N * iu;
+    g.w = dw.as<double>();
+    g.ortol_rel = 1e-7;
+    eig_bind_workspace(g, ws.ptr);
+    rc = (c.precision == FORGE_PREC_MIXED) ? eig_mixed(c.stream, g, mws.ptr) : eig_fp64(c.stream, g);
+    std::vector<int> fails(nb);
+    if (!rc) {
+        FORGE_CUDA(cudaMemcpyAsync(w, dw.ptr, nb * iu * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        if (Z) FORGE_CUDA(cudaMemcpyAsync(Z, dX.ptr, nb * N * iu * sizeof(double2), cudaMemcpyDeviceToHost, c.stream));
+        FORGE_CUDA(cudaMemcpyAsync(fails.data(), g.fail, nb * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    }
+    dA.release();
+    dX.release();
+    dw.release();
+    ws.release();
+    mws.release();
+    if (rc) return rc;
+    int bad = 0;
+    for (int64_t b = 0; b < nb; ++b) bad += fails[b] ? 1 : 0;
+    return bad;
+}
+
+int forge_gpu_solve(forge_ctx* x, const double* Potential, const double* zFock, double* Bands, double* zEigenvectors,
+                    double* zFockBulk) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    FORGE_TRY(upload_state(x, Potential, zFock));
+    int info = 0;
+    FORGE_TRY(solve_device(x, &info));
+    const int64_t N = c.N, iu = c.nUpper, Nk = c.Nk, numb = c.numb;
+    if (Bands) {
+        std::vector<double> w((size_t)Nk * iu);
+        FORGE_CUDA(cudaMemcpyAsync(w.data(), x->w.ptr, w.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        FORGE_CUDA(cudaStreamSynchronize(c.stream));
+        for (int64_t k = 0; k < Nk; ++k)
+            for (int64_t b = 0; b < numb; ++b) Bands[b + k * numb] = w[k * iu + c.nLower - 1 + b];
+    }
+    if (zEigenvectors) {
+        for (int64_t k = 0; k < Nk; ++k)
+            FORGE_CUDA(cudaMemcpyAsync(zEigenvectors + 2 * (size_t)k * N * numb,
+                                       c.X.as<double2>() + (size_t)k * N * iu + (size_t)(c.nLower - 1) * N,
+                                       (size_t)N * numb * sizeof(double2), cudaMemcpyDeviceToHost, c.stream));
+    }
+    if (zFockBulk)
+        FORGE_CUDA(cudaMemcpyAsync(zFockBulk, c.bulk.ptr, 4 * (size_t)N * N * sizeof(double2), cudaMemcpyDeviceToHost,
+                                   c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    return info;
+}
+
+int forge_gpu_sort_energies(forge_ctx* x, double* SortedEnergies, int64_t* nSortedMomenta, int64_t* nSortedIndex) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    FORGE_TRY(sort_device(x, c.s.nfilling));
+    const int64_t nw = c.numb * c.Nk;
+    std::vector<int64_t> idx(nw);
+    FORGE_CUDA(cudaMemcpyAsync(idx.data(), x->sorted_idx.ptr, nw * sizeof(int64_t), cudaMemcpyDeviceToHost, c.stream));
+    if (SortedEnergies)
+        FORGE_CUDA(cudaMemcpyAsync(SortedEnergies, x->sorted_e.ptr, nw * sizeof(double), cudaMemcpyDeviceToHost,
+                                   c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    x->h_sorted_idx = idx;
+    if (nSortedIndex) std::memcpy(nSortedIndex, idx.data(), nw * sizeof(int64_t));
+    if (nSortedMomenta) {
+        for (int64_t q = 0; q < nw; ++q) {
+            const int64_t icount = idx[q];
+            const int64_t band = (icount - 1) / c.Nk, k = icount - 1 - band * c.Nk;
+            nSortedMomenta[q] = c.kcomp[k];
+            nSortedMomenta[q + nw] = c.kcomp[k + c.Nk];
+        }
+    }
+    return 0;
+}
+
+int forge_gpu_fermi(forge_ctx* x, double nfilling, int64_t* nFermiLevel, double* FermiEnergy, int64_t* nOccStates,
+                    int64_t* nPartOccStates, double* DegFactor) {
+    FORGE_TRY(check_ctx(x));
+    FORGE_TRY(sort_device(x, nfilling));
+    ScfScalars h;
+    FORGE_TRY(read_scalars(x, &h));
+    if (nFermiLevel) *nFermiLevel = h.nF;
+    if (FermiEnergy) *FermiEnergy = h.EF;
+    if (nOccStates) *nOccStates = h.nOcc;
+    if (nPartOccStates) *nPartOccStates = h.nPart;
+    if (DegFactor) *DegFactor = h.DegFactor;
+    return 0;
+}
+
+int forge_gpu_get_fock(forge_ctx* x, double DegFactor, int64_t nOccStates, int64_t nPartOccStates, double* zFock) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!x->have_sort) {
+        set_error(FORGE_ERR_STATE, "get_fock before sort_energies");
+        return FORGE_ERR_STATE;
+    }
+    const int64_t nw = c.numb * c.Nk;
+    if (nOccStates < 0 || nOccStates > nw || nPartOccStates < 0 || nPartOccStates > nOccStates) {
+        set_error(FORGE_ERR_ARG, "get_fock: nOcc=%lld nPart=%lld out of range", (long long)nOccStates,
+                  (long long)nPartOccStates);
+        return FORGE_ERR_ARG;
+    }
+    // occupied window states with the caller's weights (HartreeFock.f90:506-555)
+    std::vector<int64_t> idx(nw);
+    FORGE_CUDA(cudaMemcpyAsync(idx.data(), x->sorted_idx.ptr, nw * sizeof(int64_t), cudaMemcpyDeviceToHost, c.stream));
+    std::vector<double2> bph(c.Nk * 4);
+    FORGE_CUDA(cudaMemcpyAsync(bph.data(), c.bphase.ptr, c.Nk * 4 * sizeof(double2), cudaMemcpyDeviceToHost, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    double2 zdeg = (c.s.degfactor_mode == FORGE_DEG_REFERENCE) ? make_double2((double)(float)DegFactor, 8.0)
+                                                                : make_double2(DegFactor, 0.0);
+    std::vector<WinState> st(nOccStates > 0 ? nOccStates : 1);
+    for (int64_t q = 0; q < nOccStates; ++q) {
+        const int64_t icount = idx[q];
+        const int64_t band = (icount - 1) / c.Nk, k = icount - 1 - band * c.Nk;
+        st[q].k = k;
+        st[q].col = c.nLower - 1 + band;
+        const double2 wgt = (q < nOccStates - nPartOccStates) ? make_double2(1.0, 0.0) : zdeg;
+        for (int t = 0; t < 4; ++t) st[q].wph[t] = cmul(bph[k * 4 + t], wgt);
+    }
+    FORGE_CUDA(cudaMemcpyAsync(x->states.ptr, st.data(), nOccStates * sizeof(WinState), cudaMemcpyHostToDevice,
+                               c.stream));
+    FORGE_TRY(get_fock_device(x, nOccStates));
+    if (zFock)
+        FORGE_CUDA(cudaMemcpyAsync(zFock, x->Pn.ptr, 4 * (size_t)c.N * c.N * sizeof(double2), cudaMemcpyDeviceToHost,
+                                   c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+int forge_gpu_energies(forge_ctx* x, const double* zFock, double* KineticEnergy, double* FockEnergy,
+                       double* HartreeEnergy, double* HubbardEnergy) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
+    const size_t NN = (size_t)c.N * c.N;
+    const double2* P = c.P.as<double2>();
+    if (zFock) {
+        FORGE_TRY(x->win.ensure(4 * NN * sizeof(double2)));
+        FORGE_CUDA(cudaMemcpyAsync(x->win.ptr, zFock, 4 * NN * sizeof(double2), cudaMemcpyHostToDevice, c.stream));
+        P = x->win.as<double2>();
+    }
+    double* d = x->dens_new.as<double>();
+    FORGE_TRY(scf_density(c, P, d));
+    ScfScalars keep;
+    FORGE_TRY(read_scalars(x, &keep));
+    FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), P, P, d, d, x->y.as<double>(), x->work.as<double>(),
+                               x->sc.as<ScfScalars>()));
+    FORGE_TRY(scf_oda(c, x->sc.as<ScfScalars>(), 1));
+    ScfScalars h;
+    FORGE_TRY(read_scalars(x, &h));
+    if (KineticEnergy) *KineticEnergy = h.Eout[0];
+    if (FockEnergy) *FockEnergy = h.Eout[1];
+    if (HartreeEnergy) *HartreeEnergy = h.Eout[2];
+    if (HubbardEnergy) *HubbardEnergy = h.Eout[3];
+    FORGE_TRY(write_scalars(x, &keep));
+    return 0;
+}
+
+int forge_gpu_optimal_step(forge_ctx* x, double* Step, double* Energies) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!x->have_pnew || !Energies) {
+        set_error(FORGE_ERR_STATE, "optimal_step needs get_fock first and an Energies array");
+        return FORGE_ERR_STATE;
+    }
+    if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
+    ScfScalars h;
+    FORGE_TRY(read_scalars(x, &h));
+    for (int t = 0; t < 4; ++t) h.Ein[t] = Energies[t];
+    FORGE_TRY(write_scalars(x, &h));
+    FORGE_TRY(scf_density(c, x->Pn.as<double2>(), x->dens_new.as<double>()));
+    FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(),
+                               x->dens_new.as<double>(), x->y.as<double>(), x->work.as<double>(),
+                               x->sc.as<ScfScalars>()));
+    FORGE_TRY(scf_oda(c, x->sc.as<ScfScalars>(), 0));
+    FORGE_TRY(read_scalars(x, &h));
+    if (Step) *Step = h.step;
+    for (int t = 0; t < 4; ++t) Energies[t] = h.Eout[t];
+    return 0;
+}
+
+int forge_gpu_mix_potential(forge_ctx* x, double Step, double* DensityConvergence, double* residual) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!x->have_pnew) {
+        set_error(FORGE_ERR_STATE, "mix_potential needs get_fock / optimal_step first");
+        return FORGE_ERR_STATE;
+    }
+    ScfScalars h;
+    FORGE_TRY(read_scalars(x, &h));
+    h.step = Step;
+    FORGE_TRY(write_scalars(x, &h));
+    FORGE_TRY(scf_mix(c, c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(), c.V.as<double>(),
+                      x->y.as<double>(), x->work.as<double>(), x->sc.as<ScfScalars>()));
+    FORGE_TRY(read_scalars(x, &h));
+    if (DensityConvergence) *DensityConvergence = h.dn_max;
+    if (residual) *residual = h.residual;
+    x->have_pnew = false;
+    return 0;
+}
+
+int forge_gpu_plain_guess(forge_ctx* x, double* Energies) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
+    const size_t NN = (size_t)c.N * c.N;
+    FORGE_CUDA(cudaMemsetAsync(c.P.ptr, 0, 4 * NN * sizeof(double2), c.stream));
+    FORGE_CUDA(cudaMemsetAsync(c.V.ptr, 0, c.N * sizeof(double), c.stream));
+    int info = 0;
+    FORGE_TRY(solve_device(x, &info));
+    // Main.f90:255: nFermiLevel without the numS factor (numS = 1 here)
+    FORGE_TRY(sort_device(x, c.s.nfilling));
+    ScfScalars h;
+    FORGE_TRY(read_scalars(x, &h));
+    FORGE_TRY(get_fock_device(x, h.nStates));
+    FORGE_CUDA(cudaMemcpyAsync(c.P.ptr, x->Pn.ptr, 4 * NN * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream));
+    x->have_pnew = false;
+    FORGE_TRY(prepare_state_device(x, Energies));
+    return info;
+}
+
+int forge_gpu_prepare_state(forge_ctx* x, double* Energies) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
+    return prepare_state_device(x, Energies);
+}
+
+int forge_gpu_scf_iteration(forge_ctx* x, double* Energies, forge_iter_report* rep) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!x->have_state) {
+        set_error(FORGE_ERR_STATE, "scf_iteration needs plain_guess or set_state + prepare_state first");
+        return FORGE_ERR_STATE;
+    }
+    if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
+    ScfScalars h;
+    FORGE_TRY(read_scalars(x, &h));
+    if (Energies) {
+        for (int t = 0; t < 4; ++t) h.Ein[t] = Energies[t];
+        FORGE_TRY(write_scalars(x, &h));
+    }
+    double Ein[4];
+    for (int t = 0; t < 4; ++t) Ein[t] = h.Ein[t];
+    int info = 0;
+    FORGE_TRY(solve_device(x, &info));
+    FORGE_TRY(sort_device(x, c.s.nfilling));
+    FORGE_TRY(read_scalars(x, &h));
+    FORGE_TRY(get_fock_device(x, h.nStates));
+    FORGE_TRY(scf_density(c, x->Pn.as<double2>(), x->dens_new.as<double>()));
+    FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(),
+                               x->dens_new.as<double>(), x->y.as<double>(), x->work.as<double>(),
+                               x->sc.as<ScfScalars>()));
+    FORGE_TRY(scf_oda(c, x->sc.as<ScfScalars>(), 0));
+    FORGE_TRY(scf_mix(c, c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(), c.V.as<double>(),
+                      x->y.as<double>(), x->work.as<double>(), x->sc.as<ScfScalars>()));
+    FORGE_TRY(read_scalars(x, &h));
+    x->have_pnew = false;
+    if (Energies)
+        for (int t = 0; t < 4; ++t) Energies[t] = h.Eout[t];
+    if (rep) {
+        rep->Step = h.step;
+        rep->DensityConvergence = h.dn_max;
+        rep->TotalEnergyIn = h.Etot_in;
+        rep->TotalEnergy = h.Etot_out;
+        rep->KineticEnergyIn = Ein[0];
+        rep->FockEnergyIn = Ein[1];
+        rep->HartreeEnergyIn = Ein[2];
+        rep->HubbardEnergyIn = Ein[3];
+        rep->KineticEnergy = h.Eout[0];
+        rep->FockEnergy = h.Eout[1];
+        rep->HartreeEnergy = h.Eout[2];
+        rep->HubbardEnergy = h.Eout[3];
+        rep->FermiEnergy = h.EF;
+        rep->DegFactor = h.DegFactor;
+        rep->residual = h.residual;
+        rep->nFermiLevel = h.nF;
+        rep->nOccStates = h.nOcc;
+        rep->nPartOccStates = h.nPart;
+        rep->info = info;
+    }
+    return info;
+}
+
+}  // extern "C"

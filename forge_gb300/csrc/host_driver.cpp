@@ -1,0 +1,347 @@
+// Host side of the SCF engine: Setup-derived parameters, geometry, and the SCF control
+// loop of FORGE's Main.f90, driving the device through the C-ABI of forge_gpu.h.
+// Compiled with -ffp-contract=off: the geometry follows the reference's unfused
+// double-precision arithmetic so that coordinates and k vectors come out bit for bit
+// as a non-FMA evaluation of Geometry.f90 / Main.f90 gives them.
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "forge_host.h"
+
+namespace {
+
+const double kA1[2] = {0.5, 0.8660254037844386};   // [0.5, sqrt(3)*0.5]  Setup.f90:71
+const double kA2[2] = {-0.5, 0.8660254037844386};  // Setup.f90:72
+
+double pi_ref() { return 4.0 * std::atan(1.0); }  // Setup.f90:74
+
+// the default-real literal 1e-6 of Geometry.f90:154
+const double kF32_1em6 = (double)1e-6f;
+
+bool ws_accept(double x1, double x2, int64_t m, double rmax) {
+    double r1 = std::fabs(x1 * (3.0 * m + 1) + x2 * (3.0 * m + 2)) + kF32_1em6;
+    double r2 = std::fabs(x1 - x2 * (3.0 * m + 1)) + kF32_1em6;
+    double r3 = std::fabs(x1 * (3.0 * m + 2) + x2) + kF32_1em6;
+    return r1 < rmax && r2 < rmax && r3 < rmax;
+}
+
+void rot(const double R[2][2], const double v[2], double out[2]) {
+    // matmul(RotMatrix, v) with RotMatrix = reshape([c,-s,s,c],[2,2]) (Main.f90:133)
+    double x = R[0][0] * v[0] + R[0][1] * v[1];
+    double y = R[1][0] * v[0] + R[1][1] * v[1];
+    out[0] = x;
+    out[1] = y;
+}
+
+}  // namespace
+
+extern "C" {
+
+int forge_host_setup(forge_setup* s) {
+    if (!s || s->nlayers < 1 || s->ntheta < 1 || s->numk < 1) return FORGE_ERR_ARG;
+    const int64_t m = s->ntheta;
+    s->ndim = s->nlayers * 2 * (m * m + (m + 1) * (m + 1) + (m + 1) * m);  // Setup.f90:10
+    s->numb = s->ndim < 20 ? s->ndim : 20;                                  // Setup.f90:23
+    const int64_t ncb = s->numb / 2;                                         // Setup.f90:24
+    s->nLower = (s->ndim - 2 * s->numb + 2 * ncb) / 2 + 1;                   // Setup.f90:67
+    s->nUpper = (s->ndim + 2 * ncb) / 2;                                     // Setup.f90:68
+    s->NeutralityPoint = (s->ndim / 2 - s->nLower) + 1;                      // Setup.f90:69
+    // Geometry.f90:14-35
+    int64_t cnt = 0;
+    for (int64_t n1 = -s->numI; n1 <= s->numI; ++n1)
+        for (int64_t n2 = -s->numI; n2 <= s->numI; ++n2)
+            if (n1 + n2 <= s->numI && n1 + n2 >= -s->numI && (n1 != 0 || n2 != 0)) ++cnt;
+    s->numNeighborCells = cnt / 2 + 1;
+    s->alpha = 5.853 / s->epsilon * 1.0;   // Setup.f90:58
+    s->alphaH = 5.853 / s->epsilon * 1.0;  // Setup.f90:59
+    s->a0 = 1.0 / std::sqrt(3.0);          // Setup.f90:62
+    s->r0 = 0.184;                         // Setup.f90:63
+    s->d0 = 1.35772 / 1.0;                 // Setup.f90:64 (pressure = 1)
+    s->tz = 1.35772 / 1.0;                 // Setup.f90:65
+    return 0;
+}
+
+int forge_host_geometry(const forge_setup* s, const int64_t* RotateLayers, double* Coords, int64_t* nUnitCell_1,
+                        int64_t* nUnitCell_2, double* tn, double* g1o, double* g12o, double* MomentaValues,
+                        int64_t* nMomentaComponents, int64_t* nMomentaFlattened, int64_t* nC2pairs,
+                        int64_t* nC3pairs, int64_t* counts) {
+    if (!s || !RotateLayers || !Coords || !nUnitCell_1 || !nUnitCell_2 || !tn || !MomentaValues ||
+        !nMomentaComponents)
+        return FORGE_ERR_ARG;
+    const int64_t N = s->ndim, m = s->ntheta, numk = s->numk, Nk = numk * numk, L = s->nlayers;
+    const double pi = pi_ref();
+    // OrderNeighborCells (Geometry.f90:40-91) for numI = 1
+    if (s->numNeighborCells != 4) return FORGE_ERR_ARG;
+    const int64_t u1[4] = {0, -1, -1, 0}, u2[4] = {0, 0, 1, -1};
+    for (int q = 0; q < 4; ++q) {
+        nUnitCell_1[q] = u1[q];
+        nUnitCell_2[q] = u2[q];
+    }
+    // reciprocal vectors and rotation (Main.f90:126-136)
+    const double aMoire = 3.0 * (double)(m * m) + 3.0 * (double)m + 1.0;
+    const double f = (4.0 * pi / 3.0) / aMoire;
+    double g1[2] = {f * ((double)(3 * m + 1) * kA1[0] + kA2[0]), f * ((double)(3 * m + 1) * kA1[1] + kA2[1])};
+    double g12[2] = {f * ((double)(3 * m + 2) * kA2[0] - kA1[0]), f * ((double)(3 * m + 2) * kA2[1] - kA1[1])};
+    const double cs = 1.0 - 1.0 / (2.0 * aMoire);
+    const double sn = std::sqrt(1.0 - cs * cs);
+    const double th = 0.5 * std::acos(cs);
+    const double c = std::cos(th), sg = std::sin(th);
+    const double R[2][2] = {{c, sg}, {-sg, c}};
+    double tmp[2];
+    rot(R, g1, tmp);
+    g1[0] = tmp[0];
+    g1[1] = tmp[1];
+    rot(R, g12, tmp);
+    g12[0] = tmp[0];
+    g12[1] = tmp[1];
+    if (g1o) {
+        g1o[0] = g1[0];
+        g1o[1] = g1[1];
+    }
+    if (g12o) {
+        g12o[0] = g12[0];
+        g12o[1] = g12[1];
+    }
+    // SampleBZ (Geometry.f90:96-127)
+    int64_t icount = 0;
+    for (int64_t ivk1 = 0; ivk1 < numk; ++ivk1)
+        for (int64_t ivk2 = 0; ivk2 < numk; ++ivk2) {
+            nMomentaComponents[icount] = ivk1;
+            nMomentaComponents[icount + Nk] = ivk2;
+            ++icount;
+            if (nMomentaFlattened) nMomentaFlattened[ivk1 + ivk2 * numk] = icount;
+        }
+    for (int64_t ivk2 = 0; ivk2 < numk; ++ivk2)
+        for (int64_t ivk1 = 0; ivk1 < numk; ++ivk1) {
+            MomentaValues[ivk1 + ivk2 * numk] = ((double)ivk1 * g1[0] + (double)ivk2 * g12[0]) / (double)numk;
+            MomentaValues[ivk1 + ivk2 * numk + Nk] = ((double)ivk1 * g1[1] + (double)ivk2 * g12[1]) / (double)numk;
+        }
+    // moire lattice vectors (Main.f90:142-144)
+    double t1[2] = {(double)m * kA1[0] + (double)(m + 1) * kA2[0], (double)m * kA1[1] + (double)(m + 1) * kA2[1]};
+    double t2[2] = {(double)(-m - 1) * kA1[0] + (double)(2 * m + 1) * kA2[0],
+                    (double)(-m - 1) * kA1[1] + (double)(2 * m + 1) * kA2[1]};
+    // WignerSeitzCell (Geometry.f90:132-273)
+    const int64_t nrad = 3 * m;
+    const double rmax = 3.0 * (double)(m * m) + 3.0 * (double)m + 1.0;
+    const double sq3 = std::sqrt(3.0);
+    int64_t nind = 0;
+    auto put = [&](double x, double y, double z) -> bool {
+        if (nind >= N) return false;
+        Coords[nind] = x;
+        Coords[nind + N] = y;
+        Coords[nind + 2 * N] = z;
+        ++nind;
+        return true;
+    };
+    for (int64_t nl = 1; nl <= L; ++nl) {
+        const double z = ((double)(float)(nl - 1) - (double)(float)(L - 1) / 2.0) * s->tz;
+        const int64_t rl = RotateLayers[nl - 1];
+        if (rl == -1) {
+            for (int64_t n1 = -nrad; n1 <= nrad; ++n1)
+                for (int64_t n2 = -nrad; n2 <= nrad; ++n2) {
+                    double an1 = n1 + 1.0 / 3.0, an2 = n2 - 2.0 / 3.0;
+                    if (ws_accept(an1, an2, m, rmax) &&
+                        !put((n1 + 1.0 / 3.0) * kA1[0] + (n2 - 2.0 / 3.0) * kA2[0],
+                             (n1 + 1.0 / 3.0) * kA1[1] + (n2 - 2.0 / 3.0) * kA2[1], z))
+                        return FORGE_ERR_ARG;
+                }
+            if (!put((-t2[0] - t1[0]) / 3.0, (-t2[1] - t1[1]) / 3.0, z)) return FORGE_ERR_ARG;
+            for (int64_t n1 = -nrad; n1 <= nrad; ++n1)
+                for (int64_t n2 = -nrad; n2 <= nrad; ++n2) {
+                    double bn1 = n1 + 2.0 / 3.0, bn2 = n2 - 1.0 / 3.0;
+                    if (ws_accept(bn1, bn2, m, rmax) &&
+                        !put(bn1 * kA1[0] + bn2 * kA2[0], bn1 * kA1[1] + bn2 * kA2[1], z))
+                        return FORGE_ERR_ARG;
+                }
+            if (!put((t2[0] + t1[0]) / 3.0, (t2[1] + t1[1]) / 3.0, z)) return FORGE_ERR_ARG;
+        } else if (rl == 1) {
+            for (int64_t n1 = -nrad; n1 <= nrad; ++n1)
+                for (int64_t n2 = -nrad; n2 <= nrad; ++n2) {
+                    double an1 = (n1 + 1.0 / 3.0) * (cs - sn / sq3) - 2 * (n2 - 2.0 / 3.0) * sn / sq3;
+                    double an2 = (n2 - 2.0 / 3.0) * (cs + sn / sq3) + 2 * (n1 + 1.0 / 3.0) * sn / sq3;
+                    if (ws_accept(an1, an2, m, rmax) &&
+                        !put(an1 * kA1[0] + an2 * kA2[0], an1 * kA1[1] + an2 * kA2[1], z))
+                        return FORGE_ERR_ARG;
+                }
+            if (!put((t1[0] + t2[0]) / 3.0, (t1[1] + t2[1]) / 3.0, z)) return FORGE_ERR_ARG;
+            for (int64_t n1 = -nrad; n1 <= nrad; ++n1)
+                for (int64_t n2 = -nrad; n2 <= nrad; ++n2) {
+                    double bn1 = (n1 + 2.0 / 3.0) * (cs - sn / sq3) - 2 * (n2 - 1.0 / 3.0) * sn / sq3;
+                    double bn2 = (n2 - 1.0 / 3.0) * (cs + sn / sq3) + 2 * (n1 + 2.0 / 3.0) * sn / sq3;
+                    if (ws_accept(bn1, bn2, m, rmax) &&
+                        !put(bn1 * kA1[0] + bn2 * kA2[0], bn1 * kA1[1] + bn2 * kA2[1], z))
+                        return FORGE_ERR_ARG;
+                }
+            if (!put((-t1[0] - t2[0]) / 3.0, (-t1[1] - t2[1]) / 3.0, z)) return FORGE_ERR_ARG;
+        } else {
+            return FORGE_ERR_ARG;
+        }
+    }
+    if (nind != N) return FORGE_ERR_ARG;
+    // rotate (x, y) by RotMatrix; z unchanged (Main.f90:148-150)
+    for (int64_t n = 0; n < N; ++n) {
+        double v[2] = {Coords[n], Coords[n + N]}, o[2];
+        rot(R, v, o);
+        Coords[n] = o[0];
+        Coords[n + N] = o[1];
+    }
+    rot(R, t1, tmp);
+    t1[0] = tmp[0];
+    t1[1] = tmp[1];
+    rot(R, t2, tmp);
+    t2[0] = tmp[0];
+    t2[1] = tmp[1];
+    tn[0] = t1[0];
+    tn[1] = t1[1];
+    tn[2] = t2[0];
+    tn[3] = t2[1];
+    tn[4] = t2[0] - t1[0];
+    tn[5] = t2[1] - t1[1];
+    // C2 / C3 site maps (Geometry.f90:1140-1223)
+    const int64_t per = N / L;
+    int64_t c2cnt = 0, c3cnt = 0;
+    if (nC2pairs) {
+        for (int64_t i = 0; i < N; ++i) nC2pairs[i] = 0;
+        for (int64_t il = 1; il <= L; ++il)
+            for (int64_t i = per * (il - 1) + 1; i <= per * (il - 1) + per / 2; ++i)
+                for (int64_t j = per * (il - 1) + per / 2 + 1; j <= per * (il - 1) + per; ++j) {
+                    double dx = Coords[i - 1] + Coords[j - 1], dy = Coords[i - 1 + N] + Coords[j - 1 + N];
+                    if (std::sqrt(dx * dx + dy * dy) < 1e-5) {
+                        nC2pairs[i - 1] = j;
+                        nC2pairs[j - 1] = i;
+                        ++c2cnt;
+                    }
+                }
+    }
+    if (nC3pairs) {
+        for (int64_t i = 0; i < N; ++i) nC3pairs[i] = 0;
+        const double sq = std::sqrt(3.0);
+        for (int64_t nl = 1; nl <= L; ++nl) {
+            const int64_t base = (nl - 1) * per;
+            const int64_t lo[2] = {base + 1, base + per / 2 + 1}, hi[2] = {base + per / 2, base + per};
+            for (int h = 0; h < 2; ++h)
+                for (int64_t i = lo[h]; i <= hi[h]; ++i) {
+                    double x = Coords[i - 1], y = Coords[i - 1 + N];
+                    double x3 = -.5 * x - .5 * sq * y, y3 = .5 * sq * x - .5 * y;
+                    for (int64_t j = lo[h]; j <= hi[h]; ++j) {
+                        double dx = Coords[j - 1] - x3, dy = Coords[j - 1 + N] - y3;
+                        if (std::sqrt(dx * dx + dy * dy) < 1e-3) {
+                            nC3pairs[i - 1] = j;
+                            ++c3cnt;
+                        }
+                    }
+                }
+        }
+        for (int64_t nl = 1; nl <= L; ++nl) {
+            nC3pairs[(nl - 1) * per + per / 2 - 1] = (nl - 1) * per + per / 2;
+            nC3pairs[(nl - 1) * per + per - 1] = (nl - 1) * per + per;
+            c3cnt += 2;
+        }
+    }
+    if (counts) {
+        counts[0] = c2cnt;
+        counts[1] = c3cnt;
+    }
+    return 0;
+}
+
+int forge_host_parameters_string(const forge_setup* s, const char* statename, char* buf, int64_t buflen) {
+    if (!s || !buf || buflen < 8) return FORGE_ERR_ARG;
+    // Main.f90:180-183
+    char dop = s->nfilling < 0.0 ? '-' : '+';
+    std::snprintf(buf, (size_t)buflen,
+                  "-%.3s-filling%c%3.1f-numS%lld-i%lld-nlayers%lld-relax0-eps%.1f-U%4.2f-screen%lld-xi%.1f-delta%.3f"
+                  "-numI%lld-numC%lld-numk%lld-dp8.dat",
+                  statename ? statename : "SSS", dop, std::fabs(s->nfilling), (long long)s->numS,
+                  (long long)s->ntheta, (long long)s->nlayers, s->epsilon, s->U, (long long)s->nscreen,
+                  s->xi * 0.246, s->Delta, (long long)s->numI, (long long)s->numC, (long long)s->numk);
+    return 0;
+}
+
+int forge_host_run_scf(forge_ctx* ctx, const forge_scf_options* opts, const double* zFock_init,
+                       forge_scf_result* result, forge_iter_report* reports) {
+    if (!ctx || !opts || !result) return FORGE_ERR_ARG;
+    std::memset(result, 0, sizeof(*result));
+    FILE* fe = nullptr;
+    FILE* fc = nullptr;
+    auto close_files = [&]() {
+        if (fe) std::fclose(fe);
+        if (fc) std::fclose(fc);
+    };
+    const bool switching = opts->mixed_until > 0 || opts->mixed_switch_tol > 0.0;
+    int rc = forge_gpu_set_precision(ctx, switching ? FORGE_PREC_MIXED : FORGE_PREC_FP64);
+    if (rc) return rc;
+    auto t0 = std::chrono::steady_clock::now();
+    double E[4];
+    if (zFock_init) {
+        if ((rc = forge_gpu_set_state(ctx, zFock_init))) return rc;
+        if ((rc = forge_gpu_prepare_state(ctx, E))) return rc;
+    } else {
+        rc = forge_gpu_plain_guess(ctx, E);
+        if (rc < 0) return rc;
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    result->guess_seconds = std::chrono::duration<double>(t1 - t0).count();
+    if (opts->output_dir) {
+        // output/Energy<parameters>, output/Convergence<parameters> (Main.f90:352-358)
+        forge_setup s;
+        char params[256];
+        if ((rc = forge_gpu_get_setup(ctx, &s))) return rc;
+        forge_host_parameters_string(&s, opts->statename, params, sizeof(params));
+        std::string d(opts->output_dir);
+        if (!d.empty() && d.back() != '/') d += '/';
+        fe = std::fopen((d + "Energy" + params).c_str(), "w");
+        fc = std::fopen((d + "Convergence" + params).c_str(), "w");
+        if (!fe || !fc) {
+            close_files();
+            return FORGE_ERR_ARG;
+        }
+    }
+    bool mixed = switching;
+    int64_t it = 0;
+    double res = 1e300;
+    while (it < opts->itmax) {
+        ++it;
+        if (mixed && ((opts->mixed_until > 0 && it > opts->mixed_until) ||
+                      (opts->mixed_switch_tol > 0.0 && res < opts->mixed_switch_tol))) {
+            mixed = false;
+            if ((rc = forge_gpu_set_precision(ctx, FORGE_PREC_FP64))) {
+                close_files();
+                return rc;
+            }
+        }
+        forge_iter_report r;
+        std::memset(&r, 0, sizeof(r));
+        rc = forge_gpu_scf_iteration(ctx, E, &r);
+        if (rc < 0) {
+            close_files();
+            return rc;
+        }
+        if (reports) reports[it - 1] = r;
+        res = r.residual;
+        if (fc)  // Main.f90:616-623
+            std::fprintf(fc, "%5.1f   %9.6f   %5.3f   %24.9f   \n", (double)it, r.DensityConvergence, r.Step,
+                         r.TotalEnergyIn - r.TotalEnergy);
+        if (fe)  // Main.f90:625-631
+            std::fprintf(fe, "%5.1f   %24.9f   %24.9f   %24.9f   %24.9f   %24.9f   \n", (double)it, r.TotalEnergyIn,
+                         2.0 * r.KineticEnergyIn, 2.0 * r.FockEnergyIn, r.HartreeEnergyIn, r.HubbardEnergyIn);
+        result->TotalEnergy = r.TotalEnergy;
+        if (opts->residual_tol > 0.0 && res < opts->residual_tol && !mixed) {
+            result->converged = 1;
+            break;
+        }
+    }
+    auto t2 = std::chrono::steady_clock::now();
+    result->iterations = it;
+    result->residual = res;
+    for (int t = 0; t < 4; ++t) result->Energies[t] = E[t];
+    result->seconds = std::chrono::duration<double>(t2 - t1).count();
+    close_files();
+    return 0;
+}
+
+}  // extern "C"

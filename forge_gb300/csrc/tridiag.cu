@@ -1,0 +1,399 @@
+// Batched Householder tridiagonalisation (see tridiag.cuh for the structure).
+//
+// Bytes per column step (algorithmic): the trailing lower triangle, (n-col)^2/2
+// complex elements, read once by trd_hemv; the rank-2k update is GEMM-shaped.
+#include "tridiag.cuh"
+#include "zgemm_engine.cuh"
+
+namespace forge {
+
+namespace {
+
+template <class V>
+__device__ inline V ldv(const V* p) {
+    return *p;
+}
+
+// Block-wide sum of a double (blockDim.x == 256).
+__device__ inline double block_sum_256(double v, double* sh) {
+    v = warp_sum_d(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x < 32) {
+        r = (l < 8) ? sh[l] : 0.0;
+        r = warp_sum_d(r);
+    }
+    __syncthreads();
+    return r;  // valid in thread 0
+}
+
+// "last CTA" detection for a per-batch counter; returns true in every thread of the last CTA.
+__device__ inline bool last_cta(unsigned* counter, unsigned total) {
+    __shared__ bool is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = atomicAdd(counter, 1u);
+        is_last = (t == total - 1);
+        if (is_last) *counter = 0u;
+    }
+    __syncthreads();
+    return is_last;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- trd_col (zlatrd column update + zlarfg)
+template <class T>
+__global__ void __launch_bounds__(TRD_ROWS) k_trd_col(TrdArgs<T> a, int64_t p, int ii, int64_t col, int has_refl) {
+    using V = typename CV<T>::type;
+    const int64_t b = blockIdx.y, n = a.n, lda = a.lda;
+    V* A = a.A + b * a.strideA;
+    V* W = a.W + b * (n * TRD_NB);
+    __shared__ V wrow[TRD_NB], arow[TRD_NB];
+    __shared__ double sh[8];
+    if (threadIdx.x < ii) {
+        wrow[threadIdx.x] = W[col + threadIdx.x * n];
+        arow[threadIdx.x] = A[col + (p + threadIdx.x) * lda];
+    }
+    __syncthreads();
+    const int64_t r = col + (int64_t)blockIdx.x * TRD_ROWS + threadIdx.x;
+    double nrm = 0.0;
+    if (r < n) {
+        V x = A[r + col * lda];
+        for (int l = 0; l < ii; ++l) {
+            x = vsub(x, vmulcj(A[r + (p + l) * lda], wrow[l]));
+            x = vsub(x, vmulcj(W[r + l * n], arow[l]));
+        }
+        if (r == col) {
+            x.y = 0;
+            a.d[b * n + col] = (double)x.x;
+        }
+        A[r + col * lda] = x;
+        double* sc = a.scal + b * 16;
+        if (r == col + 1) {
+            sc[0] = (double)x.x;
+            sc[1] = (double)x.y;
+        }
+        if (r >= col + 2) nrm = (double)x.x * (double)x.x + (double)x.y * (double)x.y;
+    }
+    double s = block_sum_256(nrm, sh);
+    double* part = a.part + b * a.pstride;
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+    if (last_cta(a.cnt + b * 4, gridDim.x) && threadIdx.x == 0) {
+        double xn2 = 0.0;
+        for (unsigned q = 0; q < gridDim.x; ++q) xn2 += ((volatile double*)part)[q];
+        double* sc = a.scal + b * 16;
+        V* tau = a.tau + b * n;
+        if (!has_refl) {
+            tau[col] = vzero<V>();
+            sc[2] = 1.0;
+            sc[3] = 0.0;
+            sc[4] = 0.0;
+            sc[5] = 0.0;
+            return;
+        }
+        const double ar = ((volatile double*)sc)[0], ai = ((volatile double*)sc)[1];
+        // zlarfg: beta = -sign(|(alpha, x)|, Re alpha), tau = (beta - alpha)/beta, x *= 1/(alpha - beta)
+        if (xn2 == 0.0 && ai == 0.0) {
+            tau[col] = vzero<V>();
+            sc[2] = 1.0;
+            sc[3] = 0.0;
+            sc[4] = 0.0;
+            sc[5] = 0.0;
+            a.e[b * n + col] = ar;
+        } else {
+            double beta = -copysign(sqrt(ar * ar + ai * ai + xn2), ar);
+            double tr = (beta - ar) / beta, ti = -ai / beta;
+            // 1/(alpha - beta)
+            double dr = ar - beta, di = ai;
+            double den = dr * dr + di * di;
+            sc[2] = dr / den;
+            sc[3] = -di / den;
+            sc[4] = tr;
+            sc[5] = ti;
+            tau[col] = vmake<V>((T)tr, (T)ti);
+            a.e[b * n + col] = beta;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- trd_hemv (+ panel dots)
+template <class T>
+__device__ inline typename CV<T>::type trd_v(const typename CV<T>::type* A, int64_t lda, int64_t col, int64_t r,
+                                             double sr, double si) {
+    using V = typename CV<T>::type;
+    if (r == col + 1) return vmake<V>((T)1, (T)0);
+    V x = A[r + col * lda];
+    return vmake<V>((T)(x.x * sr - x.y * si), (T)(x.x * si + x.y * sr));
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_trd_hemv(TrdArgs<T> a, int64_t p, int ii, int64_t col, int64_t ntiles) {
+    using V = typename CV<T>::type;
+    const int64_t b = blockIdx.y, n = a.n, lda = a.lda;
+    const V* A = a.A + b * a.strideA;
+    const double* sc = a.scal + b * 16;
+    const double sr = sc[2], si = sc[3];
+    const int64_t c0 = col + 1;
+    const int64_t t = blockIdx.x;
+    if (t < ntiles) {
+        // tile (bi, bj), bi >= bj, of the trailing matrix A(c0:n, c0:n)
+        int64_t bi = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+        while ((bi + 1) * (bi + 2) / 2 <= t) ++bi;
+        while (bi * (bi + 1) / 2 > t) --bi;
+        const int64_t bj = t - bi * (bi + 1) / 2;
+        const int64_t R0 = c0 + bi * TRD_TILE, C0 = c0 + bj * TRD_TILE;
+        __shared__ V vr[TRD_TILE], vc[TRD_TILE];
+        __shared__ V rsum[4][TRD_TILE];
+        __shared__ V csum[2][TRD_TILE];
+        if (threadIdx.x < TRD_TILE) {
+            int64_t r = R0 + threadIdx.x;
+            vr[threadIdx.x] = (r < n) ? trd_v<T>(A, lda, col, r, sr, si) : vzero<V>();
+        } else if (threadIdx.x < 2 * TRD_TILE) {
+            int64_t c = C0 + threadIdx.x - TRD_TILE;
+            vc[threadIdx.x - TRD_TILE] = (c < n) ? trd_v<T>(A, lda, col, c, sr, si) : vzero<V>();
+        }
+        __syncthreads();
+        const int tr = threadIdx.x & 63, tg = threadIdx.x >> 6;
+        const int64_t row = R0 + tr;
+        V racc = vzero<V>();
+        V cacc[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) cacc[q] = vzero<V>();
+        const bool diag = (bi == bj);
+        if (row < n) {
+            const V vrow = vr[tr];
+#pragma unroll 4
+            for (int q = 0; q < 16; ++q) {
+                const int64_t c = C0 + tg * 16 + q;
+                if (c < n && (!diag || c <= row)) {
+                    V av = A[row + c * lda];
+                    if (c == row) av.y = 0;
+                    racc = vadd(racc, vmul(av, vc[tg * 16 + q]));
+                    if (c != row) cacc[q] = vadd(cacc[q], vcjmul(av, vrow));
+                }
+            }
+        }
+        rsum[tg][tr] = racc;
+        const int lane = threadIdx.x & 31, half = (threadIdx.x >> 5) & 1;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            V s = warp_sum(cacc[q]);
+            if (lane == 0) csum[half][tg * 16 + q] = s;
+        }
+        __syncthreads();
+        V* Yrow = a.Yrow + b * a.ystride;
+        V* Ycol = a.Ycol + b * a.ystride;
+        if (threadIdx.x < TRD_TILE) {
+            int64_t r = R0 + threadIdx.x;
+            if (r < n) {
+                V s = vadd(vadd(rsum[0][threadIdx.x], rsum[1][threadIdx.x]),
+                           vadd(rsum[2][threadIdx.x], rsum[3][threadIdx.x]));
+                Yrow[bj * n + r] = s;
+            }
+        } else if (threadIdx.x < 2 * TRD_TILE) {
+            int q = threadIdx.x - TRD_TILE;
+            int64_t c = C0 + q;
+            if (c < n) Ycol[bi * n + c] = vadd(csum[0][q], csum[1][q]);
+        }
+    } else {
+        // panel dots over rows [c0 + rb*256, ...): s1 = W^H v, s2 = V^H v
+        const int64_t rb = t - ntiles;
+        const int64_t r = c0 + rb * 256 + threadIdx.x;
+        const V* W = a.W + b * (n * TRD_NB);
+        __shared__ V s1w[8][TRD_NB], s2w[8][TRD_NB];
+        V v = (r < n) ? trd_v<T>(A, lda, col, r, sr, si) : vzero<V>();
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        for (int l = 0; l < ii; ++l) {
+            V x1 = vzero<V>(), x2 = vzero<V>();
+            if (r < n) {
+                x1 = vcjmul(W[r + l * n], v);
+                x2 = vcjmul(A[r + (p + l) * lda], v);
+            }
+            x1 = warp_sum(x1);
+            x2 = warp_sum(x2);
+            if (lane == 0) {
+                s1w[w][l] = x1;
+                s2w[w][l] = x2;
+            }
+        }
+        __syncthreads();
+        V* S = a.Spart + b * a.sstride + rb * 2 * TRD_NB;
+        if (threadIdx.x < ii) {
+            V x1 = vzero<V>(), x2 = vzero<V>();
+            for (int q = 0; q < 8; ++q) {
+                x1 = vadd(x1, s1w[q][threadIdx.x]);
+                x2 = vadd(x2, s2w[q][threadIdx.x]);
+            }
+            S[threadIdx.x] = x1;
+            S[TRD_NB + threadIdx.x] = x2;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- trd_finish
+template <class T>
+__global__ void __launch_bounds__(TRD_ROWS) k_trd_finish(TrdArgs<T> a, int64_t p, int ii, int64_t col, int64_t nb2,
+                                                         int64_t nrb) {
+    using V = typename CV<T>::type;
+    const int64_t b = blockIdx.y, n = a.n, lda = a.lda;
+    V* A = a.A + b * a.strideA;
+    V* W = a.W + b * (n * TRD_NB);
+    double* sc = a.scal + b * 16;
+    const double sr = sc[2], si = sc[3];
+    const V tau = vmake<V>((T)sc[4], (T)sc[5]);
+    const int64_t c0 = col + 1;
+    __shared__ V s1[TRD_NB], s2[TRD_NB];
+    __shared__ double sh[8];
+    if (threadIdx.x < ii) {
+        const V* S = a.Spart + b * a.sstride;
+        V x1 = vzero<V>(), x2 = vzero<V>();
+        for (int64_t q = 0; q < nrb; ++q) {
+            x1 = vadd(x1, S[q * 2 * TRD_NB + threadIdx.x]);
+            x2 = vadd(x2, S[q * 2 * TRD_NB + TRD_NB + threadIdx.x]);
+        }
+        s1[threadIdx.x] = x1;
+        s2[threadIdx.x] = x2;
+    }
+    __syncthreads();
+    const int64_t r = c0 + (int64_t)blockIdx.x * TRD_ROWS + threadIdx.x;
+    double dre = 0.0, dim = 0.0;
+    if (r < n) {
+        const int64_t B = (r - c0) / TRD_TILE;
+        const V* Yrow = a.Yrow + b * a.ystride;
+        const V* Ycol = a.Ycol + b * a.ystride;
+        V y = vzero<V>();
+        for (int64_t q = 0; q <= B; ++q) y = vadd(y, Yrow[q * n + r]);
+        for (int64_t q = B; q < nb2; ++q) y = vadd(y, Ycol[q * n + r]);
+        for (int l = 0; l < ii; ++l) {
+            y = vsub(y, vmul(A[r + (p + l) * lda], s1[l]));
+            y = vsub(y, vmul(W[r + l * n], s2[l]));
+        }
+        y = vmul(tau, y);
+        V v = trd_v<T>(A, lda, col, r, sr, si);
+        A[r + col * lda] = v;
+        W[r + ii * n] = y;
+        // zdotc(w, v) = sum conj(w) v
+        V cv = vcjmul(y, v);
+        dre = (double)cv.x;
+        dim = (double)cv.y;
+    }
+    double s_re = block_sum_256(dre, sh);
+    double s_im = block_sum_256(dim, sh);
+    double* part = a.part + b * a.pstride;
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = s_re;
+        part[2 * blockIdx.x + 1] = s_im;
+    }
+    if (last_cta(a.cnt + b * 4 + 1, gridDim.x) && threadIdx.x == 0) {
+        double xr = 0.0, xi = 0.0;
+        for (unsigned q = 0; q < gridDim.x; ++q) {
+            xr += ((volatile double*)part)[2 * q];
+            xi += ((volatile double*)part)[2 * q + 1];
+        }
+        // alpha2 = -1/2 tau (w^H v)
+        const double tr = sc[4], ti = sc[5];
+        sc[6] = -0.5 * (tr * xr - ti * xi);
+        sc[7] = -0.5 * (tr * xi + ti * xr);
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(TRD_ROWS) k_trd_fix(TrdArgs<T> a, int ii, int64_t col) {
+    using V = typename CV<T>::type;
+    const int64_t b = blockIdx.y, n = a.n, lda = a.lda;
+    const V* A = a.A + b * a.strideA;
+    V* W = a.W + b * (n * TRD_NB);
+    const double* sc = a.scal + b * 16;
+    const V al = vmake<V>((T)sc[6], (T)sc[7]);
+    const int64_t r = col + 1 + (int64_t)blockIdx.x * TRD_ROWS + threadIdx.x;
+    if (r < n) W[r + ii * n] = vadd(W[r + ii * n], vmul(al, A[r + col * lda]));
+}
+
+// ---------------------------------------------------------------- rank-2k trailing update
+template <class V>
+struct Her2kA {
+    const V* A;
+    const V* W;
+    int64_t lda, strideA, n, strideW, r0, p, w;
+    __device__ V operator()(int64_t i, int64_t k) const {
+        const int64_t r = r0 + i, b = blockIdx.z;
+        if (r >= n || k >= 2 * w) return vzero<V>();
+        if (k < w) return A[b * strideA + r + (p + k) * lda];
+        return W[b * strideW + r + (k - w) * n];
+    }
+};
+template <class V>
+struct Her2kB {
+    const V* A;
+    const V* W;
+    int64_t lda, strideA, n, strideW, r0, p, w;
+    __device__ V operator()(int64_t j, int64_t k) const {
+        const int64_t r = r0 + j, b = blockIdx.z;
+        if (r >= n || k >= 2 * w) return vzero<V>();
+        if (k < w) return vconj(W[b * strideW + r + k * n]);
+        return vconj(A[b * strideA + r + (p + k - w) * lda]);
+    }
+};
+template <class V>
+struct Her2kEpi {
+    V* A;
+    int64_t lda, strideA, r0;
+    __device__ void operator()(int64_t i, int64_t j, V c) const {
+        V* x = A + blockIdx.z * strideA + (r0 + i) + (r0 + j) * lda;
+        V y = vsub(*x, c);
+        if (i == j) y.y = 0;
+        *x = y;
+    }
+};
+
+template <class T>
+int her2k_update(cudaStream_t st, TrdArgs<T>& a, int64_t p, int64_t w, int64_t batch) {
+    using V = typename CV<T>::type;
+    const int64_t r0 = p + w, m = a.n - r0;
+    if (m <= 0) return 0;
+    Her2kA<V> fa{a.A, a.W, a.lda, a.strideA, a.n, a.n * TRD_NB, r0, p, w};
+    Her2kB<V> fb{a.A, a.W, a.lda, a.strideA, a.n, a.n * TRD_NB, r0, p, w};
+    Her2kEpi<V> ep{a.A, a.lda, a.strideA, r0};
+    return zgemm_launch<V, IMAJOR, IMAJOR, true>(st, m, m, 2 * w, batch, fa, fb, ep);
+}
+
+// ---------------------------------------------------------------- driver
+template <class T>
+int tridiagonalize(cudaStream_t st, TrdArgs<T>& a, int64_t batch) {
+    const int64_t n = a.n;
+    for (int64_t p = 0; p < n; p += TRD_NB) {
+        const int64_t w = (n - p < TRD_NB) ? (n - p) : TRD_NB;
+        int64_t nrefl = 0;
+        for (int ii = 0; ii < w; ++ii) {
+            const int64_t col = p + ii;
+            const int has_refl = (col < n - 1) ? 1 : 0;
+            dim3 ga((unsigned)((n - col + TRD_ROWS - 1) / TRD_ROWS), (unsigned)batch);
+            k_trd_col<T><<<ga, TRD_ROWS, 0, st>>>(a, p, ii, col, has_refl);
+            FORGE_LAUNCH_CHECK();
+            if (!has_refl) continue;
+            ++nrefl;
+            const int64_t n2 = n - col - 1;
+            const int64_t nb2 = (n2 + TRD_TILE - 1) / TRD_TILE;
+            const int64_t ntiles = nb2 * (nb2 + 1) / 2;
+            const int64_t nrb = (n2 + 255) / 256;
+            dim3 gb((unsigned)(ntiles + (ii > 0 ? nrb : 0)), (unsigned)batch);
+            k_trd_hemv<T><<<gb, 256, 0, st>>>(a, p, ii, col, ntiles);
+            FORGE_LAUNCH_CHECK();
+            dim3 gc((unsigned)((n2 + TRD_ROWS - 1) / TRD_ROWS), (unsigned)batch);
+            k_trd_finish<T><<<gc, TRD_ROWS, 0, st>>>(a, p, ii, col, nb2, ii > 0 ? nrb : 0);
+            FORGE_LAUNCH_CHECK();
+            k_trd_fix<T><<<gc, TRD_ROWS, 0, st>>>(a, ii, col);
+            FORGE_LAUNCH_CHECK();
+        }
+        if (nrefl > 0 && p + w < n) FORGE_TRY(her2k_update<T>(st, a, p, nrefl, batch));
+    }
+    return 0;
+}
+
+template int tridiagonalize<double>(cudaStream_t, TrdArgs<double>&, int64_t);
+
+}  // namespace forge

@@ -1,0 +1,179 @@
+/*
+ * forge_gpu.h -- C-ABI of the GB300 (sm_103a) Hartree-Fock SCF engine.
+ *
+ * Drop-in boundary for the hot path of FORGE (forge-team/forge, Fortran 90):
+ * every entry point replaces one routine of HartreeFock.f90 / LapackRoutines.f90
+ * or one inline loop of Main.f90, with the same argument meaning.  A Fortran
+ * host binds these with ISO_C_BINDING (interface blocks in INTEGRATION.md).
+ *
+ * Conventions
+ *   - integers are int64_t (the reference's integer(dp)), reals are double (real(dp));
+ *   - complex arrays are interleaved (re, im) doubles, i.e. Fortran complex(dp) /
+ *     C99 double _Complex, column-major, 1-based indices in the reference map to
+ *     0-based offsets here;
+ *   - zFock-shaped arrays are ndim x ndim x numNeighborCells (Main.f90:104-106);
+ *   - a NULL host pointer for an input means "use the device-resident copy kept
+ *     by the context"; a NULL host pointer for an output means "keep it on the
+ *     device only" (no host copy);
+ *   - every call returns a status: 0 = OK, > 0 = eigen-solver info (LAPACK style,
+ *     number of k points whose solve did not converge), < 0 = FORGE_ERR_*.
+ *     forge_gpu_last_error() gives the message of the last failure.
+ *   - a context is used from one host thread at a time; all work runs on the
+ *     context's own CUDA stream.
+ */
+#ifndef FORGE_GPU_H
+#define FORGE_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    FORGE_OK = 0,
+    FORGE_ERR_ARG = -1,     /* invalid argument */
+    FORGE_ERR_CUDA = -2,    /* CUDA runtime error */
+    FORGE_ERR_STATE = -3,   /* call out of order (e.g. solve before init) */
+    FORGE_ERR_NOMEM = -4,   /* device allocation failed */
+    FORGE_ERR_TIMEOUT = -5, /* a bounded device-side wait gave up */
+    FORGE_ERR_NUMERIC = -6  /* non-finite value detected */
+};
+
+enum { FORGE_PREC_FP64 = 0, FORGE_PREC_MIXED = 1 };
+enum { FORGE_DEG_REFERENCE = 0, FORGE_DEG_CORRECTED = 1 };
+
+/* Runtime mirror of Setup.f90:6-74 (only the parameters the SCF path reads). */
+typedef struct forge_setup {
+    int64_t nlayers;          /* Setup.f90:7 */
+    int64_t ntheta;           /* Setup.f90:8 */
+    int64_t numk;             /* Setup.f90:11 */
+    int64_t numS;             /* Setup.f90:13 (only 1 is supported) */
+    int64_t numI;             /* Setup.f90:19 (only 1 is supported: 4 neighbour cells) */
+    int64_t numC;             /* Setup.f90:20 */
+    int64_t nscreen;          /* Setup.f90:21 */
+    int64_t fphase;           /* Setup.f90:25 */
+    int64_t ndim;             /* Setup.f90:10 */
+    int64_t numb;             /* Setup.f90:23 */
+    int64_t nLower, nUpper;   /* Setup.f90:67-68 */
+    int64_t NeutralityPoint;  /* Setup.f90:69 */
+    int64_t numNeighborCells; /* Geometry.f90:14-35 */
+    int64_t degfactor_mode;   /* FORGE_DEG_*: zdeg of HartreeFock.f90:529 */
+    int64_t precision;        /* FORGE_PREC_*: eigen-solver / projector arithmetic */
+    double nfilling;          /* Setup.f90:14 */
+    double U;                 /* Setup.f90:16 */
+    double epsilon;           /* Setup.f90:17 */
+    double Delta;             /* Setup.f90:18 */
+    double xi;                /* Setup.f90:22 */
+    double alpha, alphaH;     /* Setup.f90:58-59 */
+    double a0, r0, d0, tz;    /* Setup.f90:62-65 */
+    double EnergyTolerance;   /* Setup.f90:51 */
+    double StepAlternative;   /* Setup.f90:52 */
+} forge_setup;
+
+typedef struct forge_ctx forge_ctx;
+
+/* Per-iteration report of forge_gpu_scf_iteration (the Convergence / Energy
+ * lines of Main.f90:616-639 plus the Fermi bookkeeping of Main.f90:400-412). */
+typedef struct forge_iter_report {
+    double Step;              /* ODA step (HartreeFock.f90:1201-1208) */
+    double DensityConvergence;/* max |n - n_in| (Main.f90:564-571) */
+    double TotalEnergyIn, TotalEnergy;
+    double KineticEnergyIn, FockEnergyIn, HartreeEnergyIn, HubbardEnergyIn;
+    double KineticEnergy, FockEnergy, HartreeEnergy, HubbardEnergy;
+    double FermiEnergy, DegFactor;
+    double residual;          /* max change of any H_HF element (eV) */
+    int64_t nFermiLevel, nOccStates, nPartOccStates;
+    int64_t info;             /* eigen-solver info of this iteration */
+} forge_iter_report;
+
+const char* forge_gpu_last_error(void);
+int forge_gpu_version(void);
+
+/* Creates a context: uploads the geometry built by the host (Main.f90:123-154) and
+ * tabulates ft / fv for the 7 cell images (K1).  tn = [t1, t2, t3] as a 2x3 column-major
+ * array (Main.f90:249 reshape([t1,t2,t3],[2,3])). */
+int forge_gpu_init(const forge_setup* setup, const double* Coords, const int64_t* nUnitCell_1,
+                   const int64_t* nUnitCell_2, const double* tn, const double* MomentaValues,
+                   const int64_t* nMomentaComponents, forge_ctx** ctx);
+int forge_gpu_finalize(forge_ctx* ctx);
+
+/* LongRangeInteraction (HartreeFock.f90:14-53).  LongRange (ndim x ndim) may be NULL. */
+int forge_gpu_long_range(forge_ctx* ctx, double* LongRange);
+
+/* Loads zFock (and its density Re diag zFock(:,:,1)) as the current state P = zFockIn,
+ * e.g. after reading a checkpoint (Main.f90:202-234) or a learned warm start. */
+int forge_gpu_set_state(forge_ctx* ctx, const double* zFock);
+/* Copies the current state back: zFock (ndim x ndim x NNC complex), Density (ndim),
+ * Potential (ndim); any of them may be NULL. */
+int forge_gpu_get_state(forge_ctx* ctx, double* zFock, double* Density, double* Potential);
+
+/* HamiltonianHartreeFock (HartreeFock.f90:57-127) for k points [k0, k0+nk): writes the
+ * lower triangles of H(k) (ndim x ndim complex each) to H (host).  Potential / zFock NULL =
+ * device state. */
+int forge_gpu_hamiltonian(forge_ctx* ctx, const double* Potential, const double* zFock, int64_t k0,
+                          int64_t nk, double* H);
+
+/* zdiagRed (LapackRoutines.f90:381-433) on a batch of nb Hermitian matrices given in the
+ * lower triangle (ndim x ndim complex each, column-major, host): eigenvalues 1..iu in
+ * ascending order into w (iu x nb) and eigenvectors into Z (ndim x iu x nb). */
+int forge_gpu_zheevr_batch(forge_ctx* ctx, int64_t nb, const double* A, int64_t iu, double* w, double* Z);
+
+/* Solve (HartreeFock.f90:402-483): H(k) for all k, eigenpairs 1..nUpper, window bands and
+ * vectors, bulk projector zFockBulk (NOT divided by Nk, as in the reference). */
+int forge_gpu_solve(forge_ctx* ctx, const double* Potential, const double* zFock, double* Bands,
+                    double* zEigenvectors, double* zFockBulk);
+
+/* SortEnergies_1Spin (HartreeFock.f90:885-925) of the last Solve: SortedEnergies (numb*Nk),
+ * nSortedMomenta (numb*Nk x 2), nSortedIndex (numb*Nk, the reference's flattened index
+ * icount = (band-1)*Nk + k, 1-based); any output may be NULL. */
+int forge_gpu_sort_energies(forge_ctx* ctx, double* SortedEnergies, int64_t* nSortedMomenta,
+                            int64_t* nSortedIndex);
+
+/* Fermi level and degeneracy bookkeeping (Main.f90:400-412) on the last sort. */
+int forge_gpu_fermi(forge_ctx* ctx, double nfilling, int64_t* nFermiLevel, double* FermiEnergy,
+                    int64_t* nOccStates, int64_t* nPartOccStates, double* DegFactor);
+
+/* GetFock (HartreeFock.f90:487-560) followed by Main.f90:510-511: the new density matrix
+ * P_new = (window projector + zFockBulk)/Nk, kept on the device; zFock (NULL allowed)
+ * receives a host copy. */
+int forge_gpu_get_fock(forge_ctx* ctx, double DegFactor, int64_t nOccStates, int64_t nPartOccStates,
+                       double* zFock);
+
+/* GetKineticEnergy + GetFockEnergy + GetHartreeHubbardEnergy (HartreeFock.f90:1012-1145) of
+ * zFock (NULL = device state P) with Density-1/2 from Re diag zFock(:,:,1). */
+int forge_gpu_energies(forge_ctx* ctx, const double* zFock, double* KineticEnergy, double* FockEnergy,
+                       double* HartreeEnergy, double* HubbardEnergy);
+
+/* OptimalStep (HartreeFock.f90:1148-1227) on the device pair (P_new, P_in); Energies[4] holds
+ * (Kinetic, Fock, Hartree, Hubbard) of P_in on entry and of the stepped state on exit. */
+int forge_gpu_optimal_step(forge_ctx* ctx, double* Step, double* Energies);
+
+/* Main.f90:558-595: P = Step*P_new + (1-Step)*P_in, Density, DensityConvergence, Potential;
+ * P_in <- P.  residual receives the mean-field residual (NULL allowed). */
+int forge_gpu_mix_potential(forge_ctx* ctx, double Step, double* DensityConvergence, double* residual);
+
+/* Initial guess without a checkpoint (Main.f90:236-346, nRead=0): non-interacting Solve,
+ * sort, Fermi, GetFock, energies and potential.  Energies[4] as in optimal_step. */
+int forge_gpu_plain_guess(forge_ctx* ctx, double* Energies);
+
+/* After forge_gpu_set_state: energies and potential of the loaded state (Main.f90:290-346). */
+int forge_gpu_prepare_state(forge_ctx* ctx, double* Energies);
+
+/* One full SCF iteration (Main.f90:365-595) with all arrays device-resident.
+ * Energies[4] as in optimal_step (in: current, out: new). */
+int forge_gpu_scf_iteration(forge_ctx* ctx, double* Energies, forge_iter_report* report);
+
+/* Selects FORGE_PREC_FP64 or FORGE_PREC_MIXED for subsequent solves. */
+int forge_gpu_set_precision(forge_ctx* ctx, int64_t precision);
+
+/* Copies the context's setup (as passed to forge_gpu_init, with the current precision). */
+int forge_gpu_get_setup(forge_ctx* ctx, forge_setup* setup);
+
+/* Synchronises the context's stream (for host timing). */
+int forge_gpu_synchronize(forge_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FORGE_GPU_H */

@@ -1,0 +1,64 @@
+/*
+ * forge_host.h -- host side of the GB300 Hartree-Fock engine (the part of FORGE's
+ * Fortran driver that stays on the CPU: Setup.f90, Geometry.f90 and the SCF control
+ * of Main.f90), in C++ because no Fortran compiler is available for this build.
+ * A Fortran host keeps its own Setup/Geometry/Main and binds only forge_gpu.h.
+ */
+#ifndef FORGE_HOST_H
+#define FORGE_HOST_H
+
+#include <stdint.h>
+
+#include "forge_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Setup.f90:6-69: fills the derived fields (ndim, numb, nLower, nUpper, NeutralityPoint,
+ * numNeighborCells, alpha, alphaH, a0, r0, d0, tz) from the primary ones already set in *s
+ * (nlayers, ntheta, numk, numS, numI, numC, nscreen, fphase, nfilling, U, epsilon, Delta, xi,
+ * EnergyTolerance, StepAlternative, degfactor_mode, precision). */
+int forge_host_setup(forge_setup* s);
+
+/* Main.f90:102-163 with Geometry.f90:14-273 and 1140-1223.  Output arrays (column-major):
+ * Coords (ndim x 3), nUnitCell_1/2 (4), tn (2 x 3: t1, t2, t3), g1 (2), g12 (2),
+ * MomentaValues (numk x numk x 2), nMomentaComponents (Nk x 2), nMomentaFlattened (numk x numk),
+ * nC2pairs / nC3pairs (ndim, 1-based) and the two site-map counts (may be NULL). */
+int forge_host_geometry(const forge_setup* s, const int64_t* RotateLayers, double* Coords, int64_t* nUnitCell_1,
+                        int64_t* nUnitCell_2, double* tn, double* g1, double* g12, double* MomentaValues,
+                        int64_t* nMomentaComponents, int64_t* nMomentaFlattened, int64_t* nC2pairs,
+                        int64_t* nC3pairs, int64_t* counts);
+
+typedef struct forge_scf_options {
+    int64_t itmax;              /* Setup.f90:53 */
+    double residual_tol;        /* > 0: stop once the mean-field residual is below it (eV) */
+    int64_t mixed_until;        /* iterations run with FORGE_PREC_MIXED before switching to FP64 (0 = never) */
+    double mixed_switch_tol;    /* > 0: switch to FP64 once the residual is below this (eV) */
+    const char* output_dir;     /* NULL: no Energy / Convergence files */
+    const char* statename;      /* label of the solution (Setup.f90:15), NULL = "SSS" */
+} forge_scf_options;
+
+typedef struct forge_scf_result {
+    int64_t iterations;
+    int64_t converged;
+    double TotalEnergy;
+    double Energies[4];         /* Kinetic, Fock, Hartree, Hubbard of the final state */
+    double residual;
+    double seconds;             /* wall time of the SCF loop (after the initial guess) */
+    double guess_seconds;       /* wall time of the initial guess */
+} forge_scf_result;
+
+/* Main.f90:236-679 (numS = 1): initial guess (plain, or zFock_init when not NULL), energies,
+ * potential, then the SCF loop with ODA mixing.  reports (may be NULL) receives one entry per
+ * iteration (capacity opts->itmax). */
+int forge_host_run_scf(forge_ctx* ctx, const forge_scf_options* opts, const double* zFock_init,
+                       forge_scf_result* result, forge_iter_report* reports);
+
+/* The parameter string of Main.f90:180-183 used in output file names. */
+int forge_host_parameters_string(const forge_setup* s, const char* statename, char* buf, int64_t buflen);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FORGE_HOST_H */

@@ -1,0 +1,76 @@
+"""CPU tests of the host side: the library builds and exports every declared entry point,
+the C++ host geometry is bit-exact with the oracle, the parameter string follows Main.f90."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import forge_oracle as fo
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    names = set()
+    for h in ("forge_gpu.h", "forge_host.h"):
+        txt = open(os.path.join(ROOT, "include", h)).read()
+        names |= set(re.findall(r"^\s*(?:int|const char\*)\s+(forge_\w+)\s*\(", txt, flags=re.M))
+    return names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    declared = _declared_symbols()
+    assert len(declared) >= 25
+    for name in sorted(declared):
+        assert hasattr(lib, name), name
+
+
+def test_library_calls_fail_cleanly_without_context(lib):
+    # argument checks run before any device work
+    assert lib.forge_gpu_solve(None, None, None, None, None, None) < 0
+    assert lib.forge_gpu_finalize(None) == 0
+    assert lib.forge_gpu_version() == 1
+
+
+@pytest.mark.parametrize("m,L,rl,numk", [(1, 2, (-1, 1), 3), (5, 2, (-1, 1), 6), (12, 3, (-1, 1, -1), 6),
+                                         (31, 2, (-1, 1), 4)])
+def test_host_geometry_bit_exact_with_oracle(lib, m, L, rl, numk):
+    import forge_gb300 as fg
+    g = fg.build_geometry(fg.Setup(ntheta=m, nlayers=L, RotateLayers=rl, numk=numk))
+    go = fo.build_geometry(fo.Setup(ntheta=m, nlayers=L, RotateLayers=rl, numk=numk))
+    assert np.array_equal(g.Coords, go.coords)
+    assert np.array_equal(g.MomentaValues, go.kvals)
+    assert np.array_equal(g.nMomentaComponents, go.kcomp)
+    assert np.array_equal(g.nMomentaFlattened, go.kflat)
+    assert np.array_equal(g.tn[:, 0], go.t1) and np.array_equal(g.tn[:, 1], go.t2) and np.array_equal(g.tn[:, 2], go.t3)
+    assert np.array_equal(g.g1, go.g1) and np.array_equal(g.g12, go.g12)
+    assert np.array_equal(g.nC2pairs, go.c2pairs) and np.array_equal(g.nC3pairs, go.c3pairs)
+    assert (g.c2_count, g.c3_count) == (go.c2_count, go.c3_count)
+    assert list(g.nUnitCell_1) == [0, -1, -1, 0] and list(g.nUnitCell_2) == [0, 0, 1, -1]
+
+
+def test_host_setup_matches_setup_f90(lib):
+    import forge_gb300 as fg
+    s = fg.Setup(ntheta=31, numk=4, nfilling=2.0, epsilon=10.0).to_struct()
+    assert (s.ndim, s.numb, s.nLower, s.nUpper, s.NeutralityPoint, s.numNeighborCells) == (11908, 20, 5945, 5964,
+                                                                                            10, 4)
+    assert s.alpha == 5.853 / 10.0 and s.tz == 1.35772 and s.r0 == 0.184
+
+
+def test_parameters_string(lib):
+    import forge_gb300 as fg
+    p = fg.parameters_string(fg.Setup(ntheta=9, numk=6))
+    assert p == "-SSS-filling+0.0-numS1-i9-nlayers2-relax0-eps10.0-U4.00-screen2-xi10.0-delta0.000-numI1-numC3-numk6-dp8.dat"
+    p = fg.parameters_string(fg.Setup(ntheta=20, numk=8, nfilling=-2.0, epsilon=8.0), "AB1")
+    assert p.startswith("-AB1-filling-2.0-numS1-i20-") and "-eps8.0-" in p
+
+
+def test_init_without_gpu_reports_error(lib):
+    from conftest import gpu_available
+    if gpu_available():
+        pytest.skip("a GPU is present")
+    import forge_gb300 as fg
+    with pytest.raises(fg.ForgeError):
+        fg.HartreeFock(fg.Setup(ntheta=1, numk=2))
