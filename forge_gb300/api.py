@@ -86,6 +86,11 @@ SIGNATURES = {
     "forge_gpu_set_precision": [_P, _I],
     "forge_gpu_get_setup": [_P, _P],
     "forge_gpu_synchronize": [_P],
+    "forge_gpu_profile": [_P, _I],
+    "forge_gpu_timer_mark": [_P, _I],
+    "forge_gpu_timer_elapsed": [_P, _I, _I, _P],
+    "forge_gpu_profile_read": [_P, _P, _P, _P, _P, _I],
+    "forge_gpu_selftest_tc_gemm": [_I, _I, _I, _I, _P, _P, _P],
     "forge_host_setup": [_P],
     "forge_host_geometry": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "forge_host_run_scf": [_P, _P, _P, _P, _P],
@@ -110,6 +115,8 @@ def load_library(path: Optional[str] = None):
         f.restype = C.c_int
     lib.forge_gpu_last_error.restype = C.c_char_p
     lib.forge_gpu_last_error.argtypes = []
+    lib.forge_gpu_launch_count.restype = C.c_int64
+    lib.forge_gpu_launch_count.argtypes = []
     if path is None:
         _LIB = lib
     return lib
@@ -383,3 +390,27 @@ class HartreeFock:
 
     def synchronize(self):
         _check(self.lib.forge_gpu_synchronize(self.ctx))
+
+    STAGES = ("tables", "long_range", "assemble", "trd_col", "hemv", "trd_finish", "her2k", "bisect", "invit",
+              "backtransform", "projector", "window", "sort", "energy", "lr_matvec", "mix", "refine")
+
+    def mark(self, slot: int):
+        """Records a CUDA event in `slot` on the context's stream."""
+        _check(self.lib.forge_gpu_timer_mark(self.ctx, slot))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_double()
+        _check(self.lib.forge_gpu_timer_elapsed(self.ctx, a, b, C.byref(ms)))
+        return ms.value
+
+    def profile(self, enable: bool = True):
+        """Resets and enables (or disables) per-stage CUDA-event timing on the context stream."""
+        _check(self.lib.forge_gpu_profile(self.ctx, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        n = len(self.STAGES)
+        ms, b, f = np.zeros(n), np.zeros(n), np.zeros(n)
+        nl = np.zeros(n, np.int64)
+        self.lib.forge_gpu_profile_read(self.ctx, _ptr(ms), _ptr(nl), _ptr(b), _ptr(f), n)
+        return {s: dict(ms=float(ms[i]), launches=int(nl[i]), bytes=float(b[i]), flops=float(f[i]))
+                for i, s in enumerate(self.STAGES)}

@@ -150,8 +150,12 @@ int launch_assemble(Context& c, const double* dV, const double2* dP, int64_t k0,
     a.nk = nk;
     a.H = dH;
     const unsigned nt = (unsigned)((c.N + ASM_T - 1) / ASM_T);
+    prof_begin(ST_ASSEMBLE);
     k_assemble<<<dim3(nt, nt), dim3(ASM_T, 8), 0, c.stream>>>(a);
     FORGE_LAUNCH_CHECK();
+    // algorithmic bytes: all H(k) lower triangles written + P(R) read once
+    const double N = (double)c.N;
+    prof_end(ST_ASSEMBLE, nk * N * (N + 1) / 2 * 16.0 + 4.0 * N * N * 16.0, 0.0);
     return 0;
 }
 

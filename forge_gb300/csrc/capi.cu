@@ -1,6 +1,7 @@
 // C-ABI entry points (include/forge_gpu.h): one per reference routine of the SCF
 // path, plus a fused device-resident iteration.  Host code here is compiled with
 // -ffp-contract=off so that the k.R phases follow the reference's unfused dot product.
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
@@ -24,6 +25,9 @@ void set_error(int code, const char* fmt, ...) {
     g_errcode = code;
 }
 int last_error_code() { return g_errcode; }
+
+static std::atomic<int64_t> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 int DevBuf::ensure(size_t nbytes) {
     if (nbytes <= bytes && ptr) return 0;
@@ -68,6 +72,8 @@ using namespace forge;
 
 struct forge_ctx {
     Context c;
+    Profiler prof;
+    cudaEvent_t marks[64] = {};
     DevBuf te;           // energy tables
     DevBuf Pn, win;      // P_new, window accumulator / scratch
     DevBuf eigws, mixws; // eigen-solver workspaces
@@ -84,6 +90,8 @@ int check_ctx(forge_ctx* x) {
         set_error(FORGE_ERR_ARG, "null context");
         return FORGE_ERR_ARG;
     }
+    x->prof.stream = x->c.stream;
+    set_current_profiler(&x->prof);
     return 0;
 }
 
@@ -248,6 +256,7 @@ int prepare_state_device(forge_ctx* x, double* Energies) {
 extern "C" {
 
 const char* forge_gpu_last_error(void) { return g_err.c_str(); }
+int64_t forge_gpu_launch_count(void) { return g_launches.load(); }
 int forge_gpu_version(void) { return 1; }
 
 int forge_gpu_init(const forge_setup* s, const double* Coords, const int64_t* nUnitCell_1, const int64_t* nUnitCell_2,
@@ -311,6 +320,8 @@ int forge_gpu_init(const forge_setup* s, const double* Coords, const int64_t* nU
         delete x;
         return FORGE_ERR_CUDA;
     }
+    x->prof.stream = c.stream;
+    set_current_profiler(&x->prof);
     const int64_t N = c.N, Nk = c.Nk, numk = s->numk;
     // phases: exp(-i k.R_c) with the floating-point dot (HartreeFock.f90:90) and the integer
     // Bloch phase exp(-2 pi i (ivk1 n1 + ivk2 n1 + ivk2 n2)/numk) (HartreeFock.f90:471)
@@ -365,6 +376,10 @@ int forge_gpu_finalize(forge_ctx* x) {
     if (!x) return 0;
     Context& c = x->c;
     if (c.stream) cudaStreamSynchronize(c.stream);
+    x->prof.release();
+    if (current_profiler() == &x->prof) set_current_profiler(nullptr);
+    for (cudaEvent_t& e : x->marks)
+        if (e) cudaEventDestroy(e);
     DevBuf* bufs[] = {&c.coords, &c.tab_t, &c.tab_v, &c.LR, &c.P, &c.P_in, &c.P_new, &c.bulk, &c.V, &c.dens,
                       &c.dens_in, &c.V_old, &c.H, &c.X, &c.bands, &c.evals, &c.kvecs, &c.kphase, &c.bphase,
                       &c.sort_idx, &c.sort_e, &c.red, &c.scalars, &x->te, &x->Pn, &x->win, &x->eigws, &x->mixws,
@@ -397,6 +412,50 @@ int forge_gpu_get_setup(forge_ctx* x, forge_setup* s) {
     *s = x->c.s;
     s->precision = x->c.precision;
     return 0;
+}
+
+int forge_gpu_timer_mark(forge_ctx* x, int64_t slot) {
+    FORGE_TRY(check_ctx(x));
+    if (slot < 0 || slot >= 64) {
+        set_error(FORGE_ERR_ARG, "timer slot %lld out of range", (long long)slot);
+        return FORGE_ERR_ARG;
+    }
+    if (!x->marks[slot]) FORGE_CUDA(cudaEventCreate(&x->marks[slot]));
+    FORGE_CUDA(cudaEventRecord(x->marks[slot], x->c.stream));
+    return 0;
+}
+
+int forge_gpu_timer_elapsed(forge_ctx* x, int64_t a, int64_t b, double* ms) {
+    FORGE_TRY(check_ctx(x));
+    if (a < 0 || a >= 64 || b < 0 || b >= 64 || !x->marks[a] || !x->marks[b] || !ms) {
+        set_error(FORGE_ERR_ARG, "timer slots not recorded");
+        return FORGE_ERR_ARG;
+    }
+    FORGE_CUDA(cudaEventSynchronize(x->marks[b]));
+    float t = 0.f;
+    FORGE_CUDA(cudaEventElapsedTime(&t, x->marks[a], x->marks[b]));
+    *ms = t;
+    return 0;
+}
+
+int forge_gpu_profile(forge_ctx* x, int64_t enable) {
+    FORGE_TRY(check_ctx(x));
+    x->prof.reset();
+    x->prof.enabled = enable != 0;
+    return 0;
+}
+
+int forge_gpu_profile_read(forge_ctx* x, double* ms, int64_t* launches, double* bytes, double* flops, int64_t n) {
+    FORGE_TRY(check_ctx(x));
+    x->prof.collect();
+    const int64_t m = n < ST_COUNT ? n : ST_COUNT;
+    for (int64_t s = 0; s < m; ++s) {
+        if (ms) ms[s] = x->prof.ms[s];
+        if (launches) launches[s] = x->prof.launches[s];
+        if (bytes) bytes[s] = x->prof.bytes[s];
+        if (flops) flops[s] = x->prof.flops[s];
+    }
+    return (int)ST_COUNT;
 }
 
 int forge_gpu_synchronize(forge_ctx* x) {

@@ -43,6 +43,7 @@ size_t eig_workspace_bytes(int64_t n, int64_t iu, int64_t batch);
 void eig_bind_workspace(EigArgs& g, void* base);
 
 int eig_fp64(cudaStream_t st, EigArgs& g);
+int tridiag_eigvecs(cudaStream_t st, EigArgs& g);
 int backtransform_fp64(cudaStream_t st, const double2* A, int64_t lda, int64_t strideA, const double2* tau, int64_t n,
                        double2* X, int64_t ldx, int64_t strideX, int64_t iu, int64_t batch, double2* Gws,
                        double2* Tws, double2* Wws, double2* W2ws);

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/forge_gpu.h"
+#include "profiler.cuh"
 
 namespace forge {
 
@@ -62,8 +63,12 @@ int last_error_code();
         }                                                                                       \
     } while (0)
 
+// every kernel launch site ends with FORGE_LAUNCH_CHECK(), which also counts the launch
+void count_launch();
+
 #define FORGE_LAUNCH_CHECK()                                                                    \
     do {                                                                                        \
+        ::forge::count_launch();                                                                \
         cudaError_t e_ = cudaGetLastError();                                                    \
         if (e_ != cudaSuccess) {                                                                \
             ::forge::set_error(FORGE_ERR_CUDA, "%s:%d launch: %s", __FILE__, __LINE__,          \

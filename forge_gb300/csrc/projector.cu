@@ -49,7 +49,10 @@ struct ProjEpi {
 int bulk_projector_fp64(cudaStream_t st, const double2* X, int64_t ldx, int64_t N, int64_t K, const double2 ph[4],
                         double2* P) {
     ProjEpi ep{P, N, {ph[0], ph[1], ph[2], ph[3]}};
-    return zgemm_launch<double2, IMAJOR, IMAJOR, true>(st, N, N, K, 1, ProjA{X, ldx, N, K}, ProjB{X, ldx, N, K}, ep);
+    prof_begin(ST_PROJECTOR);
+    int rc = zgemm_launch<double2, IMAJOR, IMAJOR, true>(st, N, N, K, 1, ProjA{X, ldx, N, K}, ProjB{X, ldx, N, K}, ep);
+    prof_end(ST_PROJECTOR, (double)N * K * 16.0 + 4.0 * 2.0 * N * N * 16.0, 4.0 * (double)N * N * K);
+    return rc;
 }
 
 struct WinA {  // a(i, s) = conj(psi_s(i)) * w_s * ph_c(k_s),  c = blockIdx.z
@@ -85,10 +88,13 @@ struct WinEpi {
 int window_projector_fp64(cudaStream_t st, const WinState* states, int64_t nstates, const double2* X, int64_t ldx,
                           int64_t strideX, int64_t N, double2* P) {
     if (nstates <= 0) return 0;
-    return zgemm_launch<double2, IMAJOR, IMAJOR, false>(st, N, N, nstates, 4,
-                                                        WinA{states, X, ldx, strideX, N, nstates},
-                                                        WinB{states, X, ldx, strideX, N, nstates},
-                                                        WinEpi{P, N});
+    prof_begin(ST_WINDOW);
+    int rc = zgemm_launch<double2, IMAJOR, IMAJOR, false>(st, N, N, nstates, 4,
+                                                          WinA{states, X, ldx, strideX, N, nstates},
+                                                          WinB{states, X, ldx, strideX, N, nstates},
+                                                          WinEpi{P, N});
+    prof_end(ST_WINDOW, (double)N * nstates * 16.0 + 4.0 * 2.0 * N * N * 16.0, 4.0 * 8.0 * (double)N * N * nstates);
+    return rc;
 }
 
 }  // namespace forge

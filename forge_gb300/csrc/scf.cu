@@ -214,8 +214,10 @@ int launch_sort_fermi(Context& c, const double* w, double nfilling, double* sort
         return FORGE_ERR_ARG;
     }
     FORGE_CUDA(cudaFuncSetAttribute(k_sort_fermi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    prof_begin(ST_SORT);
     k_sort_fermi<<<1, 256, smem, c.stream>>>(a);
     FORGE_LAUNCH_CHECK();
+    prof_end(ST_SORT, (double)(c.numb * c.Nk) * 32.0, 0.0);
     return 0;
 }
 
@@ -483,14 +485,20 @@ __global__ void k_potential(const double* __restrict__ y, const double* __restri
 int scf_energy_forms(Context& c, const double* te, const double2* Pa, const double2* Pb, const double* da,
                      const double* db, double* y, double* work, ScfScalars* sc) {
     const int64_t N = c.N;
+    const double NN = (double)N * N;
+    prof_begin(ST_ENERGY);
     k_energy_pass<<<RED_CTAS, 256, 0, c.stream>>>(te, Pa, Pb, N, c.s.alpha, work);
     FORGE_LAUNCH_CHECK();
     k_reduce_forms<<<1, 32, 0, c.stream>>>(work, RED_CTAS, sc);
     FORGE_LAUNCH_CHECK();
+    // 8 tables + two 4-cell complex states read once
+    prof_end(ST_ENERGY, 8.0 * NN * 8.0 + 2.0 * 4.0 * NN * 16.0, 4.0 * NN * 14.0);
     double* part = work + RED_CTAS * 8;
     dim3 g((unsigned)((N + 255) / 256), LR_CHUNKS);
+    prof_begin(ST_LRMATVEC);
     k_lr_matvec<<<g, 256, 0, c.stream>>>(c.LR.as<double>(), da, db, N, part);
     FORGE_LAUNCH_CHECK();
+    prof_end(ST_LRMATVEC, NN * 8.0, 4.0 * NN);
     double* hpart = part + (size_t)LR_CHUNKS * 2 * N;
     const unsigned nb = (unsigned)((N + 255) / 256);
     k_lr_finish<<<nb, 256, 0, c.stream>>>(part, da, db, N, y, hpart);
@@ -517,8 +525,10 @@ int scf_mix(Context& c, double2* P, const double2* Pn, double* dens, double* V, 
     FORGE_LAUNCH_CHECK();
     k_mix_finish<<<1, 32, 0, c.stream>>>(work, (int)nb, sc);
     FORGE_LAUNCH_CHECK();
+    prof_begin(ST_MIX);
     k_mix_p<<<1216, 256, 0, c.stream>>>(P, Pn, 4 * (size_t)N * N, sc);
     FORGE_LAUNCH_CHECK();
+    prof_end(ST_MIX, 3.0 * 4.0 * (double)N * N * 16.0, 0.0);
     return 0;
 }
 

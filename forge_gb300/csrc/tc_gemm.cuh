@@ -1,0 +1,256 @@
+// tcgen05 (5th-generation tensor core) GEMM for sm_103a, TF32 inputs, FP32 accumulation in TMEM.
+//
+//   D[b](m, n) = sum_k A[b](m, k) * B[b](n, k)        (both operands K-major, fp32 storage read as tf32)
+//
+// One CTA (128 threads) per 128 x 128 output tile:
+//   warp 0 / lane 0 : TMA producer (cp.async.bulk.tensor.3d, 128B swizzle, 4-stage ring)
+//   warp 1 / lane 0 : MMA issuer   (tcgen05.mma.cta_group::1.kind::tf32, M=128 N=128 K=8)
+//   all 4 warps     : epilogue     (tcgen05.ld.32x32b.x32 -> registers -> functor)
+// TMEM: 128 columns allocated by warp 0.  Every mbarrier wait is bounded; on timeout the
+// kernel raises an error flag, stops issuing, drains, frees its TMEM and returns.
+//
+// Complex products run as real GEMMs over operands staged by the callers (real/imag planes,
+// and hi/lo TF32 splits for FP32-accurate results: a*b ~ ah*bh + ah*bl + al*bh).
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "forge_internal.cuh"
+
+namespace forge {
+
+constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 32, TC_STAGES = 4, TC_THREADS = 128;
+constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 4;  // 16 KB per operand per stage
+constexpr int TC_SMEM = TC_STAGES * 2 * TC_TILE_BYTES + 1024 + 256;
+constexpr uint32_t TC_SPIN_LIMIT = 1u << 26;     // bounded waits (>> any legitimate wait)
+
+struct TcOperand {
+    const float* ptr;
+    int64_t rows, cols;      // rows = M (or N), cols = K (elements, contiguous)
+    int64_t ld;              // row pitch in elements (multiple of 4)
+    int64_t batch_stride;    // elements between batch entries
+};
+
+// Builds the 3D TMA descriptor {K, rows, batch} with a 32 x 128 box and 128B swizzle.
+int tc_make_tmap(CUtensorMap* map, const TcOperand& op, int64_t batch);
+
+__device__ inline uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ inline void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ inline void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ inline void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// returns false if the wait gave up
+__device__ inline bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < TC_SPIN_LIMIT; ++it) {
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (abort_flag && (it & 1023u) == 1023u && *abort_flag) return false;
+    }
+    return false;
+}
+
+__device__ inline void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int32_t x, int32_t y,
+                                   int32_t z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
+        "[%2];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+        : "memory");
+}
+
+// UMMA shared-memory descriptor: K-major, 128B swizzle, 8-row groups 1024 B apart.
+__device__ inline uint64_t umma_desc_sw128(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);          // start address
+    d |= (uint64_t)1 << 16;                          // leading byte offset (unused for SW128 K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;                // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                          // descriptor version (sm_100 family)
+    d |= (uint64_t)2 << 61;                          // layout: SWIZZLE_128B
+    return d;
+}
+
+// instruction descriptor: kind::tf32, D = F32, A = B = TF32, both K-major, M = 128, N = 128
+constexpr uint32_t tc_idesc_tf32() {
+    return (1u << 4)                       // D format F32
+           | (2u << 7)                     // A format TF32
+           | (2u << 10)                    // B format TF32
+           | ((uint32_t)(TC_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+}
+
+__device__ inline void tc_mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ inline void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+template <class EPI>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_tc_gemm_tf32(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int64_t M,
+                   int64_t N, int64_t K, EPI epi, int* err) {
+    extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+    unsigned char* base = (unsigned char*)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
+    float* sA = (float*)base;
+    float* sB = (float*)(base + TC_STAGES * TC_TILE_BYTES);
+    uint64_t* bars = (uint64_t*)(base + 2 * TC_STAGES * TC_TILE_BYTES);
+    uint64_t* full = bars;                  // TMA -> MMA
+    uint64_t* empty = bars + TC_STAGES;     // MMA -> TMA
+    uint64_t* accum = bars + 2 * TC_STAGES; // MMA -> epilogue
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * TC_STAGES + 1);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+    volatile int* n_issued = abort_flag + 1;    // k blocks whose TMA loads were issued
+    volatile int* n_consumed = abort_flag + 2;  // k blocks consumed by the MMA issuer
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t m0 = (int64_t)blockIdx.x * TC_BM, n0 = (int64_t)blockIdx.y * TC_BN, b = blockIdx.z;
+    const int nk = (int)((K + TC_BK - 1) / TC_BK);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accum, 1);
+        *abort_flag = 0;
+        *n_issued = 0;
+        *n_consumed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"((uint32_t)TC_BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0) {
+        // ---- TMA producer
+        for (int kb = 0; kb < nk; ++kb) {
+            const int s = kb % TC_STAGES;
+            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
+            if (kb >= TC_STAGES && !mbar_wait(&empty[s], ph ^ 1u, abort_flag)) {
+                *abort_flag = 1;
+                break;
+            }
+            if (*abort_flag) break;
+            mbar_expect_tx(&full[s], 2 * TC_TILE_BYTES);
+            tma_load_3d(sA + s * (TC_TILE_BYTES / 4), &mapA, &full[s], kb * TC_BK, (int32_t)m0, (int32_t)b);
+            tma_load_3d(sB + s * (TC_TILE_BYTES / 4), &mapB, &full[s], kb * TC_BK, (int32_t)n0, (int32_t)b);
+            *n_issued = kb + 1;
+        }
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer
+        const uint32_t idesc = tc_idesc_tf32();
+        for (int kb = 0; kb < nk; ++kb) {
+            const int s = kb % TC_STAGES;
+            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
+            if (!mbar_wait(&full[s], ph, abort_flag)) {
+                *abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a0 = smem_u32(sA + s * (TC_TILE_BYTES / 4)), b0 = smem_u32(sB + s * (TC_TILE_BYTES / 4));
+#pragma unroll
+            for (int kk = 0; kk < TC_BK / 8; ++kk) {
+                // K = 8 tf32 = 32 bytes per MMA: advance the start address inside the 128B swizzle atom
+                tc_mma_tf32(tmem, umma_desc_sw128(a0 + kk * 32), umma_desc_sw128(b0 + kk * 32), idesc,
+                            (kb > 0 || kk > 0) ? 1u : 0u);
+            }
+            tc_commit(&empty[s]);  // frees the stage once these MMAs have read it
+            *n_consumed = kb + 1;
+        }
+        // arrives once every MMA issued above has completed (immediately if none was issued)
+        tc_commit(accum);
+    }
+    __syncwarp();
+    // ---- epilogue: all 4 warps
+    const bool acc_ok = mbar_wait(accum, 0, abort_flag);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!acc_ok || *abort_flag) {
+        if (threadIdx.x == 0) {
+            atomicExch(err, 1);
+            // drain: the MMAs in flight (accum) and the TMA loads issued but not consumed
+            mbar_wait(accum, 0, nullptr);
+            for (int kb = *n_consumed; kb < *n_issued; ++kb)
+                mbar_wait(&full[kb % TC_STAGES], (uint32_t)(kb / TC_STAGES) & 1u, nullptr);
+        }
+    } else if (nk > 0) {
+        const int64_t row = m0 + warp * 32 + lane;
+        for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+            uint32_t r[32];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                  "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                  "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            float v[32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
+            epi(b, row, n0 + c0, v, M, N);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)TC_BN));
+    }
+}
+
+// Host launcher: D tiles for b < batch; the epilogue gets (b, row, col0, v[32], M, N) and must
+// bounds-check row < M and col0 + q < N itself.
+template <class EPI>
+int tc_gemm_tf32(cudaStream_t st, const TcOperand& A, const TcOperand& B, int64_t K, int64_t batch, const EPI& epi,
+                 int* err) {
+    if (A.rows <= 0 || B.rows <= 0 || batch <= 0) return 0;
+    if ((A.ld % 4) || (B.ld % 4) || (A.batch_stride % 4) || (B.batch_stride % 4) ||
+        ((uintptr_t)A.ptr % 16) || ((uintptr_t)B.ptr % 16)) {
+        set_error(FORGE_ERR_ARG, "tc_gemm: operands must be 16-byte aligned with pitches multiple of 4 floats");
+        return FORGE_ERR_ARG;
+    }
+    CUtensorMap ma, mb;
+    TcOperand a = A, bb = B;
+    a.cols = K;
+    bb.cols = K;
+    FORGE_TRY(tc_make_tmap(&ma, a, batch));
+    FORGE_TRY(tc_make_tmap(&mb, bb, batch));
+    static bool attr_set = false;
+    if (!attr_set) {
+        FORGE_CUDA(cudaFuncSetAttribute(k_tc_gemm_tf32<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+        attr_set = true;
+    }
+    dim3 grd((unsigned)((A.rows + TC_BM - 1) / TC_BM), (unsigned)((B.rows + TC_BN - 1) / TC_BN), (unsigned)batch);
+    k_tc_gemm_tf32<EPI><<<grd, TC_THREADS, TC_SMEM, st>>>(ma, mb, A.rows, B.rows, K, epi, err);
+    FORGE_LAUNCH_CHECK();
+    return 0;
+}
+
+}  // namespace forge

@@ -477,22 +477,36 @@ int eig_fp64(cudaStream_t st, EigArgs& g) {
     a.cnt = g.cnt;
     FORGE_CUDA(cudaMemsetAsync(g.cnt, 0, sizeof(unsigned) * 4 * batch, st));
     FORGE_TRY(tridiagonalize<double>(st, a, batch));
+    FORGE_TRY(tridiag_eigvecs(st, g));
+    prof_begin(ST_BACKTRANSFORM);
+    FORGE_TRY(backtransform_fp64(st, g.A, g.lda, g.strideA, g.tau, n, g.X, g.ldx, g.strideX, iu, batch, g.G, g.T,
+                                 g.Wb, g.W2b));
+    prof_end(ST_BACKTRANSFORM, batch * (double)n * iu * 16.0 * 2.0 + batch * 0.5 * n * (double)n * 16.0,
+             batch * 8.0 * (double)n * n * iu);
+    return 0;
+}
+
+// eigenvalues 1..iu (bisection) and tridiagonal eigenvectors (inverse iteration) into g.X (real)
+int tridiag_eigvecs(cudaStream_t st, EigArgs& g) {
+    const int64_t n = g.n, iu = g.iu, batch = g.batch;
     k_gersh<<<(unsigned)batch, 256, 0, st>>>(g.d, g.e, n, g.info);
     FORGE_LAUNCH_CHECK();
     dim3 gb((unsigned)((iu + 127) / 128), (unsigned)batch);
+    prof_begin(ST_BISECT);
     k_bisect<<<gb, 128, 0, st>>>(g.d, g.e, n, iu, g.info, g.w);
     FORGE_LAUNCH_CHECK();
+    prof_end(ST_BISECT, batch * 16.0 * n, batch * 10.0 * 60.0 * (double)n * iu);
     k_clusters<<<(unsigned)batch, 32, 0, st>>>(g.w, iu, g.info, g.ortol_rel, g.clus);
     FORGE_LAUNCH_CHECK();
     FORGE_CUDA(cudaMemsetAsync(g.fail, 0, sizeof(int) * batch, st));
     dim3 gi((unsigned)((g.scr_stride + 63) / 64), (unsigned)batch);
+    prof_begin(ST_INVIT);
     k_invit<<<gi, 64, 0, st>>>(g.d, g.e, n, iu, g.w, g.info, g.clus, g.Z, g.scr, g.pivs, g.scr_stride, g.fail);
     FORGE_LAUNCH_CHECK();
+    prof_end(ST_INVIT, batch * 8.0 * (double)n * iu, 0.0);
     dim3 gz((unsigned)((n + 31) / 32), (unsigned)((iu + 31) / 32), (unsigned)batch);
     k_z_to_x<<<gz, dim3(32, 8), 0, st>>>(g.Z, n, iu, g.X, g.ldx, g.strideX);
     FORGE_LAUNCH_CHECK();
-    FORGE_TRY(backtransform_fp64(st, g.A, g.lda, g.strideA, g.tau, n, g.X, g.ldx, g.strideX, iu, batch, g.G, g.T,
-                                 g.Wb, g.W2b));
     return 0;
 }
 

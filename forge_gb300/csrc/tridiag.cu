@@ -371,9 +371,12 @@ int tridiagonalize(cudaStream_t st, TrdArgs<T>& a, int64_t batch) {
         for (int ii = 0; ii < w; ++ii) {
             const int64_t col = p + ii;
             const int has_refl = (col < n - 1) ? 1 : 0;
+            const double esz = (double)sizeof(typename CV<T>::type);
             dim3 ga((unsigned)((n - col + TRD_ROWS - 1) / TRD_ROWS), (unsigned)batch);
+            prof_begin(ST_TRD_COL);
             k_trd_col<T><<<ga, TRD_ROWS, 0, st>>>(a, p, ii, col, has_refl);
             FORGE_LAUNCH_CHECK();
+            prof_end(ST_TRD_COL, batch * (double)(n - col) * (2.0 * ii + 2.0) * esz, 0.0);
             if (!has_refl) continue;
             ++nrefl;
             const int64_t n2 = n - col - 1;
@@ -381,15 +384,26 @@ int tridiagonalize(cudaStream_t st, TrdArgs<T>& a, int64_t batch) {
             const int64_t ntiles = nb2 * (nb2 + 1) / 2;
             const int64_t nrb = (n2 + 255) / 256;
             dim3 gb((unsigned)(ntiles + (ii > 0 ? nrb : 0)), (unsigned)batch);
+            prof_begin(ST_HEMV);
             k_trd_hemv<T><<<gb, 256, 0, st>>>(a, p, ii, col, ntiles);
             FORGE_LAUNCH_CHECK();
+            // algorithmic traffic: the trailing lower triangle read once
+            prof_end(ST_HEMV, batch * 0.5 * (double)n2 * (double)(n2 + 1) * esz, batch * 8.0 * (double)n2 * n2);
             dim3 gc((unsigned)((n2 + TRD_ROWS - 1) / TRD_ROWS), (unsigned)batch);
+            prof_begin(ST_TRD_FINISH);
             k_trd_finish<T><<<gc, TRD_ROWS, 0, st>>>(a, p, ii, col, nb2, ii > 0 ? nrb : 0);
             FORGE_LAUNCH_CHECK();
             k_trd_fix<T><<<gc, TRD_ROWS, 0, st>>>(a, ii, col);
             FORGE_LAUNCH_CHECK();
+            prof_end(ST_TRD_FINISH, batch * (double)n2 * (2.0 * ii + 4.0) * esz, 0.0);
         }
-        if (nrefl > 0 && p + w < n) FORGE_TRY(her2k_update<T>(st, a, p, nrefl, batch));
+        if (nrefl > 0 && p + w < n) {
+            const double m2 = (double)(n - p - w);
+            prof_begin(ST_HER2K);
+            FORGE_TRY(her2k_update<T>(st, a, p, nrefl, batch));
+            prof_end(ST_HER2K, batch * m2 * m2 * (double)sizeof(typename CV<T>::type),
+                     batch * 8.0 * m2 * m2 * (double)nrefl);  // lower half of 2*nrefl complex MACs
+        }
     }
     return 0;
 }

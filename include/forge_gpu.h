@@ -89,6 +89,8 @@ typedef struct forge_iter_report {
 
 const char* forge_gpu_last_error(void);
 int forge_gpu_version(void);
+/* Number of kernels this library has launched in the process so far (all contexts). */
+int64_t forge_gpu_launch_count(void);
 
 /* Creates a context: uploads the geometry built by the host (Main.f90:123-154) and
  * tabulates ft / fv for the 7 cell images (K1).  tn = [t1, t2, t3] as a 2x3 column-major
@@ -169,6 +171,25 @@ int forge_gpu_set_precision(forge_ctx* ctx, int64_t precision);
 
 /* Copies the context's setup (as passed to forge_gpu_init, with the current precision). */
 int forge_gpu_get_setup(forge_ctx* ctx, forge_setup* setup);
+
+/* Stage timing with CUDA events on the context's stream (no counterpart in the reference,
+ * which has no timers).  forge_gpu_profile(ctx, 1) resets and enables it; profile_read fills
+ * up to n entries per stage (milliseconds, launches, algorithmic bytes and flops) in the
+ * order: tables, long_range, assemble, trd_col, hemv, trd_finish, her2k, bisect, invit,
+ * backtransform, projector, window, sort, energy, lr_matvec, mix, refine; returns the
+ * number of stages. */
+int forge_gpu_profile(forge_ctx* ctx, int64_t enable);
+/* Records a CUDA event in slot (0..63) on the context stream / elapsed ms between two slots. */
+int forge_gpu_timer_mark(forge_ctx* ctx, int64_t slot);
+int forge_gpu_timer_elapsed(forge_ctx* ctx, int64_t slot_a, int64_t slot_b, double* ms);
+int forge_gpu_profile_read(forge_ctx* ctx, double* ms, int64_t* launches, double* bytes, double* flops,
+                           int64_t n);
+
+/* Diagnostic (no counterpart in the reference): D = A B^T on the tcgen05 tensor cores with
+ * TF32 inputs and FP32 accumulation; A (batch x M x K), B (batch x N x K), D (batch x M x N),
+ * all row-major fp32 host arrays.  Used by the tests to validate the tensor-core GEMM. */
+int forge_gpu_selftest_tc_gemm(int64_t M, int64_t N, int64_t K, int64_t batch, const float* A, const float* B,
+                               float* D);
 
 /* Synchronises the context's stream (for host timing). */
 int forge_gpu_synchronize(forge_ctx* ctx);

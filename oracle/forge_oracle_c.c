@@ -132,3 +132,81 @@ void fo_rank1_projector(int64_t N, int64_t nb, const double* Z, int64_t ldz, dou
         }
     }
 }
+
+/* HamiltonianHartreeFock (HartreeFock.f90:57-127) for one k with ft / fv evaluated per pair as the
+ * reference does (no tables): H lower triangle, column-major N x N interleaved complex.
+ * P: zFock (N x N x 4, column-major interleaved).  cell c = 1..3 shifts R_c = n1 t1 + n2 t2. */
+void fo_hamiltonian_k(int64_t N, const double* coords /* N x 3 row-major */, const int64_t* u1, const int64_t* u2,
+                      const double* t1, const double* t2, const fo_model* p, double alpha, const double* V,
+                      const double* P, const double* vk, double* H) {
+    const size_t NN = (size_t)N * N;
+    double ph[4][2];
+    for (int c = 1; c < 4; ++c) {
+        double rx = u1[c] * t1[0] + u2[c] * t2[0], ry = u1[c] * t1[1] + u2[c] * t2[1];
+        double th = vk[0] * rx + vk[1] * ry;
+        ph[c][0] = cos(th);
+        ph[c][1] = -sin(th); /* exp(-i k.R) */
+    }
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int64_t j = 0; j < N; ++j) {
+        const double* rj = coords + 3 * j;
+        for (int64_t i = j; i < N; ++i) {
+            const double* ri = coords + 3 * i;
+            const size_t oij = i + j * (size_t)N, oji = j + i * (size_t)N;
+            double hr = (i == j) ? V[i] : 0.0, hi = 0.0;
+            double v0 = fo_fv(p, ri, rj[0], rj[1], rj[2]);
+            hr += -alpha * v0 * P[2 * oij];
+            hi += alpha * v0 * P[2 * oij + 1];
+            hr += fo_ft(p, ri, rj[0], rj[1], rj[2]);
+            for (int c = 1; c < 4; ++c) {
+                const double n1 = (double)u1[c], n2 = (double)u2[c];
+                const double er = ph[c][0], ei = ph[c][1];
+                double xm = rj[0] - n1 * t1[0] - n2 * t2[0], ym = rj[1] - n1 * t1[1] - n2 * t2[1];
+                double xp = rj[0] + n1 * t1[0] + n2 * t2[0], yp = rj[1] + n1 * t1[1] + n2 * t2[1];
+                double tm = fo_ft(p, ri, xm, ym, rj[2]), tp = fo_ft(p, ri, xp, yp, rj[2]);
+                hr += tm * er + tp * er;
+                hi += tm * ei - tp * ei;
+                double vm = fo_fv(p, ri, xm, ym, rj[2]);
+                double rs[3] = {rj[0], rj[1], rj[2]};
+                double vt = fo_fv(p, rs, ri[0] - n1 * t1[0] - n2 * t2[0], ri[1] - n1 * t1[1] - n2 * t2[1], ri[2]);
+                const double* pc = P + 2 * (c * NN);
+                double ar = pc[2 * oij], ai = -pc[2 * oij + 1]; /* conj(P_c(i,j)) */
+                hr += -alpha * vm * (ar * er - ai * ei);
+                hi += -alpha * vm * (ar * ei + ai * er);
+                double br = pc[2 * oji], bi = pc[2 * oji + 1]; /* P_c(j,i) e^{+ikR} */
+                hr += -alpha * vt * (br * er + bi * ei);
+                hi += -alpha * vt * (bi * er - br * ei);
+            }
+            H[2 * oij] = hr;
+            H[2 * oij + 1] = hi;
+        }
+    }
+}
+
+/* GetKineticEnergy + GetFockEnergy (HartreeFock.f90:1012-1145) with ft / fv per pair. out[0]=kinetic, out[1]=fock */
+void fo_energies_kf(int64_t N, const double* coords, const int64_t* u1, const int64_t* u2, const double* t1,
+                    const double* t2, const fo_model* p, const double* P, double* out) {
+    const size_t NN = (size_t)N * N;
+    double ek = 0.0, ef = 0.0;
+#pragma omp parallel for schedule(dynamic, 8) reduction(+ : ek, ef)
+    for (int64_t i = 0; i < N; ++i) {
+        const double* ri = coords + 3 * i;
+        for (int64_t j = 0; j < N; ++j) {
+            const double* rj = coords + 3 * j;
+            const size_t oij = i + j * (size_t)N, oji = j + i * (size_t)N;
+            ek += fo_ft(p, ri, rj[0], rj[1], rj[2]) * P[2 * oij];
+            ef += -0.5 * fo_fv(p, ri, rj[0], rj[1], rj[2]) * (P[2 * oij] * P[2 * oij] + P[2 * oij + 1] * P[2 * oij + 1]);
+            for (int c = 1; c < 4; ++c) {
+                const double n1 = (double)u1[c], n2 = (double)u2[c];
+                double xm = rj[0] - n1 * t1[0] - n2 * t2[0], ym = rj[1] - n1 * t1[1] - n2 * t2[1];
+                double xp = rj[0] + n1 * t1[0] + n2 * t2[0], yp = rj[1] + n1 * t1[1] + n2 * t2[1];
+                const double* pc = P + 2 * (c * NN);
+                ek += fo_ft(p, ri, xm, ym, rj[2]) * pc[2 * oij] + fo_ft(p, ri, xp, yp, rj[2]) * pc[2 * oji];
+                ef += -0.5 * fo_fv(p, ri, xm, ym, rj[2]) * (pc[2 * oij] * pc[2 * oij] + pc[2 * oij + 1] * pc[2 * oij + 1]);
+                ef += -0.5 * fo_fv(p, ri, xp, yp, rj[2]) * (pc[2 * oji] * pc[2 * oji] + pc[2 * oji + 1] * pc[2 * oji + 1]);
+            }
+        }
+    }
+    out[0] = ek;
+    out[1] = ef;
+}

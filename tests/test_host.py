@@ -16,7 +16,7 @@ def _declared_symbols():
     names = set()
     for h in ("forge_gpu.h", "forge_host.h"):
         txt = open(os.path.join(ROOT, "include", h)).read()
-        names |= set(re.findall(r"^\s*(?:int|const char\*)\s+(forge_\w+)\s*\(", txt, flags=re.M))
+        names |= set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(forge_\w+)\s*\(", txt, flags=re.M))
     return names
 
 
