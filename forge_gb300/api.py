@@ -91,6 +91,14 @@ SIGNATURES = {
     "forge_gpu_timer_elapsed": [_P, _I, _I, _P],
     "forge_gpu_profile_read": [_P, _P, _P, _P, _P, _I],
     "forge_gpu_selftest_tc_gemm": [_I, _I, _I, _I, _P, _P, _P],
+    "forge_gpu_mlp_create": [_I, _I, C.c_uint64, _P],
+    "forge_gpu_mlp_destroy": [_P],
+    "forge_gpu_mlp_set_params": [_P, _P],
+    "forge_gpu_mlp_get_params": [_P, _P, _P],
+    "forge_gpu_mlp_set_loss_weights": [_P, _P],
+    "forge_gpu_mlp_forward": [_P, _P, _I, _P],
+    "forge_gpu_mlp_gradient": [_P, _P, _P, _I, _P, _P],
+    "forge_gpu_mlp_train": [_P, _P, _P, _I, _I, _I, _D, C.c_uint64, _P],
     "forge_host_setup": [_P],
     "forge_host_geometry": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "forge_host_run_scf": [_P, _P, _P, _P, _P],
@@ -117,6 +125,8 @@ def load_library(path: Optional[str] = None):
     lib.forge_gpu_last_error.argtypes = []
     lib.forge_gpu_launch_count.restype = C.c_int64
     lib.forge_gpu_launch_count.argtypes = []
+    lib.forge_gpu_mlp_num_params.restype = C.c_int64
+    lib.forge_gpu_mlp_num_params.argtypes = [_P]
     if path is None:
         _LIB = lib
     return lib

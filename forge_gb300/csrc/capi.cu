@@ -78,12 +78,16 @@ struct forge_ctx {
     DevBuf Pn, win;      // P_new, window accumulator / scratch
     DevBuf eigws, mixws; // eigen-solver workspaces
     DevBuf states, sorted_e, sorted_idx, sc, work, y, dens_new, w;
+    DevBuf projws, tcerr;  // tensor-core projector staging and its error flag
     int64_t eig_batch = 0;
-    bool have_solve = false, have_sort = false, have_pnew = false, have_state = false;
+    bool have_solve = false, have_sort = false, have_pnew = false, have_state = false, bulk_is_fused = false;
     std::vector<int64_t> h_sorted_idx;
+    std::vector<double2> h_bph;
 };
 
 namespace {
+
+int read_scalars(forge_ctx* x, ScfScalars* h);
 
 int check_ctx(forge_ctx* x) {
     if (!x) {
@@ -166,28 +170,88 @@ int eig_batch_run(forge_ctx* x, int64_t k0, int64_t nb, int* info) {
     return 0;
 }
 
-// full Solve on the device: H(k), eigenpairs, bulk projector (not divided by Nk)
-int solve_device(forge_ctx* x, int* info) {
+// bulk_c += ph_c(k) conj(X_k) X_k^T over the first K columns (precision of the context)
+int project_k(forge_ctx* x, int64_t k, int64_t K, const double2* ph, double2* out) {
+    Context& c = x->c;
+    const int64_t N = c.N, iu = c.nUpper;
+    const double2* Xk = c.X.as<double2>() + (size_t)k * N * iu;
+    if (c.precision == FORGE_PREC_MIXED) {
+        FORGE_TRY(x->projws.ensure(proj_tc_workspace_floats(N, iu) * sizeof(float)));
+        FORGE_TRY(x->tcerr.ensure(sizeof(int)));
+        return bulk_projector_tc(c.stream, Xk, N, N, K, iu, ph, out, x->projws.as<float>(), x->tcerr.as<int>());
+    }
+    return bulk_projector_fp64(c.stream, Xk, N, N, K, ph, out);
+}
+
+// full Solve on the device: H(k), eigenpairs, and (with_projector) the bulk projector of bands
+// 1..nLower-1 (not divided by Nk), as Solve returns it
+int solve_device(forge_ctx* x, int* info, bool with_projector = true) {
     Context& c = x->c;
     FORGE_TRY(ensure_solve_buffers(x));
-    const int64_t N = c.N, iu = c.nUpper, Nk = c.Nk, B = x->eig_batch;
+    const int64_t N = c.N, Nk = c.Nk, B = x->eig_batch;
     const size_t NN = (size_t)N * N;
     FORGE_CUDA(cudaMemsetAsync(c.bulk.ptr, 0, 4 * NN * sizeof(double2), c.stream));
     *info = 0;
-    std::vector<double2> bph(Nk * 4);
-    FORGE_CUDA(cudaMemcpyAsync(bph.data(), c.bphase.ptr, Nk * 4 * sizeof(double2), cudaMemcpyDeviceToHost, c.stream));
+    x->h_bph.resize(Nk * 4);
+    FORGE_CUDA(cudaMemcpyAsync(x->h_bph.data(), c.bphase.ptr, Nk * 4 * sizeof(double2), cudaMemcpyDeviceToHost,
+                               c.stream));
     FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    if (x->tcerr.ptr) FORGE_CUDA(cudaMemsetAsync(x->tcerr.ptr, 0, sizeof(int), c.stream));
     for (int64_t k0 = 0; k0 < Nk; k0 += B) {
         const int64_t nb = (Nk - k0 < B) ? Nk - k0 : B;
         FORGE_TRY(launch_assemble(c, c.V.as<double>(), c.P.as<double2>(), k0, nb, c.H.as<double2>()));
         FORGE_TRY(eig_batch_run(x, k0, nb, info));
-        for (int64_t k = k0; k < k0 + nb; ++k) {
-            const double2* Xk = c.X.as<double2>() + (size_t)k * N * iu;
-            FORGE_TRY(bulk_projector_fp64(c.stream, Xk, N, N, c.nLower - 1, &bph[k * 4], c.bulk.as<double2>()));
-        }
+        if (with_projector)
+            for (int64_t k = k0; k < k0 + nb; ++k)
+                FORGE_TRY(project_k(x, k, c.nLower - 1, &x->h_bph[k * 4], c.bulk.as<double2>()));
     }
     x->have_solve = true;
     x->have_sort = false;
+    x->bulk_is_fused = !with_projector;
+    return 0;
+}
+
+// P_new = (sum over k of the projector onto bands 1..nLower-1 plus the fully occupied window bands
+// of k, plus the partially occupied states with weight zdeg) / Nk: the sum Main.f90:506-511
+// forms as GetFock + zFockBulk, with the weight-1 window states folded into each k's product.
+int project_fused(forge_ctx* x) {
+    Context& c = x->c;
+    const int64_t N = c.N, Nk = c.Nk;
+    const size_t NN = (size_t)N * N;
+    ScfScalars h;
+    FORGE_TRY(read_scalars(x, &h));
+    const int64_t nocc = h.nOcc, npart = h.nPart;
+    std::vector<WinState> st(nocc > 0 ? nocc : 1);
+    if (nocc > 0)
+        FORGE_CUDA(cudaMemcpyAsync(st.data(), x->states.ptr, nocc * sizeof(WinState), cudaMemcpyDeviceToHost,
+                                   c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    std::vector<int64_t> fk(Nk, 0);
+    for (int64_t q = 0; q < nocc - npart; ++q) fk[st[q].k] += 1;
+    FORGE_TRY(x->Pn.ensure(4 * NN * sizeof(double2)));
+    FORGE_CUDA(cudaMemsetAsync(x->Pn.ptr, 0, 4 * NN * sizeof(double2), c.stream));
+    if (x->tcerr.ptr) FORGE_CUDA(cudaMemsetAsync(x->tcerr.ptr, 0, sizeof(int), c.stream));
+    for (int64_t k = 0; k < Nk; ++k)
+        FORGE_TRY(project_k(x, k, c.nLower - 1 + fk[k], &x->h_bph[k * 4], x->Pn.as<double2>()));
+    if (npart > 0) {
+        // partially occupied states (complex weight zdeg in reference mode): full N x N products
+        FORGE_CUDA(cudaMemcpyAsync(x->states.ptr, st.data() + (nocc - npart), npart * sizeof(WinState),
+                                   cudaMemcpyHostToDevice, c.stream));
+        FORGE_TRY(window_projector_fp64(c.stream, x->states.as<WinState>(), npart, c.X.as<double2>(), c.N,
+                                        c.N * c.nUpper, c.N, x->Pn.as<double2>()));
+    }
+    FORGE_CUDA(cudaMemsetAsync(c.bulk.ptr, 0, 4 * NN * sizeof(double2), c.stream));
+    FORGE_TRY(scf_combine(c, x->Pn.as<double2>(), c.bulk.as<double2>()));
+    if (x->tcerr.ptr) {
+        int herr = 0;
+        FORGE_CUDA(cudaMemcpyAsync(&herr, x->tcerr.ptr, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        FORGE_CUDA(cudaStreamSynchronize(c.stream));
+        if (herr) {
+            set_error(FORGE_ERR_TIMEOUT, "tcgen05 projector: a bounded mbarrier wait gave up");
+            return FORGE_ERR_TIMEOUT;
+        }
+    }
+    x->have_pnew = true;
     return 0;
 }
 
@@ -383,7 +447,8 @@ int forge_gpu_finalize(forge_ctx* x) {
     DevBuf* bufs[] = {&c.coords, &c.tab_t, &c.tab_v, &c.LR, &c.P, &c.P_in, &c.P_new, &c.bulk, &c.V, &c.dens,
                       &c.dens_in, &c.V_old, &c.H, &c.X, &c.bands, &c.evals, &c.kvecs, &c.kphase, &c.bphase,
                       &c.sort_idx, &c.sort_e, &c.red, &c.scalars, &x->te, &x->Pn, &x->win, &x->eigws, &x->mixws,
-                      &x->states, &x->sorted_e, &x->sorted_idx, &x->sc, &x->work, &x->y, &x->dens_new, &x->w};
+                      &x->states, &x->sorted_e, &x->sorted_idx, &x->sc, &x->work, &x->y, &x->dens_new, &x->w,
+                      &x->projws, &x->tcerr};
     for (DevBuf* b : bufs) b->release();
     if (c.stream) cudaStreamDestroy(c.stream);
     delete x;
@@ -759,12 +824,10 @@ int forge_gpu_plain_guess(forge_ctx* x, double* Energies) {
     FORGE_CUDA(cudaMemsetAsync(c.P.ptr, 0, 4 * NN * sizeof(double2), c.stream));
     FORGE_CUDA(cudaMemsetAsync(c.V.ptr, 0, c.N * sizeof(double), c.stream));
     int info = 0;
-    FORGE_TRY(solve_device(x, &info));
+    FORGE_TRY(solve_device(x, &info, false));
     // Main.f90:255: nFermiLevel without the numS factor (numS = 1 here)
     FORGE_TRY(sort_device(x, c.s.nfilling));
-    ScfScalars h;
-    FORGE_TRY(read_scalars(x, &h));
-    FORGE_TRY(get_fock_device(x, h.nStates));
+    FORGE_TRY(project_fused(x));
     FORGE_CUDA(cudaMemcpyAsync(c.P.ptr, x->Pn.ptr, 4 * NN * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream));
     x->have_pnew = false;
     FORGE_TRY(prepare_state_device(x, Energies));
@@ -795,10 +858,9 @@ int forge_gpu_scf_iteration(forge_ctx* x, double* Energies, forge_iter_report* r
     double Ein[4];
     for (int t = 0; t < 4; ++t) Ein[t] = h.Ein[t];
     int info = 0;
-    FORGE_TRY(solve_device(x, &info));
+    FORGE_TRY(solve_device(x, &info, false));
     FORGE_TRY(sort_device(x, c.s.nfilling));
-    FORGE_TRY(read_scalars(x, &h));
-    FORGE_TRY(get_fock_device(x, h.nStates));
+    FORGE_TRY(project_fused(x));
     FORGE_TRY(scf_density(c, x->Pn.as<double2>(), x->dens_new.as<double>()));
     FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(),
                                x->dens_new.as<double>(), x->y.as<double>(), x->work.as<double>(),

@@ -24,8 +24,9 @@ int tc_make_tmap(CUtensorMap* map, const TcOperand& op, int64_t batch) {
         set_error(FORGE_ERR_CUDA, "cuTensorMapEncodeTiled not available from the driver");
         return FORGE_ERR_CUDA;
     }
-    const int64_t bstride = (batch > 1) ? op.batch_stride : op.rows * op.ld;
-    cuuint64_t dims[3] = {(cuuint64_t)op.cols, (cuuint64_t)op.rows, (cuuint64_t)batch};
+    const int64_t planes = op.nplanes > 0 ? op.nplanes : batch;
+    const int64_t bstride = (planes > 1) ? op.batch_stride : op.rows * op.ld;
+    cuuint64_t dims[3] = {(cuuint64_t)op.cols, (cuuint64_t)op.rows, (cuuint64_t)planes};
     cuuint64_t strides[2] = {(cuuint64_t)op.ld * 4, (cuuint64_t)bstride * 4};
     cuuint32_t box[3] = {(cuuint32_t)TC_BK, (cuuint32_t)TC_BM, 1};
     cuuint32_t estr[3] = {1, 1, 1};

@@ -28,12 +28,30 @@ constexpr uint32_t TC_SPIN_LIMIT = 1u << 26;     // bounded waits (>> any legiti
 
 struct TcOperand {
     const float* ptr;
-    int64_t rows, cols;      // rows = M (or N), cols = K (elements, contiguous)
+    int64_t rows, cols;      // rows = M (or N), cols = K extent of one plane (elements, contiguous)
     int64_t ld;              // row pitch in elements (multiple of 4)
-    int64_t batch_stride;    // elements between batch entries
+    int64_t batch_stride;    // elements between planes (3rd TMA dimension)
+    int64_t nplanes = 0;     // extent of the 3rd dimension (0: = batch)
 };
 
-// Builds the 3D TMA descriptor {K, rows, batch} with a 32 x 128 box and 128B swizzle.
+// K-block -> TMA coordinate map of one operand.  The GEMM's K runs over nseg segments of
+// nkp blocks of 32; segment s reads plane zsel[s] (+ zbatch * batch index) starting at
+// element koff of each row.  A plain operand is nseg = 1, zsel = {0}, zbatch = 1.
+struct TcKMap {
+    int32_t nkp, nseg, koff, zbatch;
+    int32_t zsel[8];
+};
+
+__host__ __device__ inline TcKMap tc_kmap_plain(int64_t K) {
+    TcKMap m{};
+    m.nkp = (int32_t)((K + 31) / 32);
+    m.nseg = 1;
+    m.koff = 0;
+    m.zbatch = 1;
+    return m;
+}
+
+// Builds the 3D TMA descriptor {K, rows, planes} with a 32 x 128 box and 128B swizzle.
 int tc_make_tmap(CUtensorMap* map, const TcOperand& op, int64_t batch);
 
 __device__ inline uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -106,7 +124,9 @@ __device__ inline void tc_commit(uint64_t* bar) {
 template <class EPI>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_tc_gemm_tf32(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int64_t M,
-                   int64_t N, int64_t K, EPI epi, int* err) {
+                   int64_t N, TcKMap ka, TcKMap kb_map, int64_t lower_div, EPI epi, int* err) {
+    // lower_div > 0: skip tiles whose rows (divided by lower_div) all lie above the diagonal
+    if (lower_div > 0 && ((int64_t)blockIdx.x * TC_BM + TC_BM - 1) / lower_div < (int64_t)blockIdx.y * TC_BN) return;
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
     float* sA = (float*)base;
@@ -122,7 +142,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t m0 = (int64_t)blockIdx.x * TC_BM, n0 = (int64_t)blockIdx.y * TC_BN, b = blockIdx.z;
-    const int nk = (int)((K + TC_BK - 1) / TC_BK);
+    const int nk = ka.nkp * ka.nseg;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TC_STAGES; ++s) {
@@ -156,8 +176,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             if (*abort_flag) break;
             mbar_expect_tx(&full[s], 2 * TC_TILE_BYTES);
-            tma_load_3d(sA + s * (TC_TILE_BYTES / 4), &mapA, &full[s], kb * TC_BK, (int32_t)m0, (int32_t)b);
-            tma_load_3d(sB + s * (TC_TILE_BYTES / 4), &mapB, &full[s], kb * TC_BK, (int32_t)n0, (int32_t)b);
+            {
+                const int sa = kb / ka.nkp, ra = kb - sa * ka.nkp;
+                const int sb = kb / kb_map.nkp, rb = kb - sb * kb_map.nkp;
+                tma_load_3d(sA + s * (TC_TILE_BYTES / 4), &mapA, &full[s], ka.koff + ra * TC_BK, (int32_t)m0,
+                            ka.zsel[sa] + ka.zbatch * (int32_t)b);
+                tma_load_3d(sB + s * (TC_TILE_BYTES / 4), &mapB, &full[s], kb_map.koff + rb * TC_BK, (int32_t)n0,
+                            kb_map.zsel[sb] + kb_map.zbatch * (int32_t)b);
+            }
             *n_issued = kb + 1;
         }
     } else if (warp == 1 && lane == 0) {
@@ -226,31 +252,45 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 }
 
 // Host launcher: D tiles for b < batch; the epilogue gets (b, row, col0, v[32], M, N) and must
-// bounds-check row < M and col0 + q < N itself.
+// bounds-check row < M and col0 + q < N itself.  Both K maps must cover the same number of
+// K blocks.  Every TMA x coordinate (koff + 32 j) is a multiple of 4 floats (16 bytes).
 template <class EPI>
-int tc_gemm_tf32(cudaStream_t st, const TcOperand& A, const TcOperand& B, int64_t K, int64_t batch, const EPI& epi,
-                 int* err) {
+int tc_gemm_tf32_mapped(cudaStream_t st, const TcOperand& A, const TcKMap& ka, const TcOperand& B, const TcKMap& kb,
+                        int64_t batch, int64_t lower_div, const EPI& epi, int* err) {
     if (A.rows <= 0 || B.rows <= 0 || batch <= 0) return 0;
-    if ((A.ld % 4) || (B.ld % 4) || (A.batch_stride % 4) || (B.batch_stride % 4) ||
+    if ((A.ld % 4) || (B.ld % 4) || (A.batch_stride % 4) || (B.batch_stride % 4) || (ka.koff % 4) || (kb.koff % 4) ||
         ((uintptr_t)A.ptr % 16) || ((uintptr_t)B.ptr % 16)) {
         set_error(FORGE_ERR_ARG, "tc_gemm: operands must be 16-byte aligned with pitches multiple of 4 floats");
         return FORGE_ERR_ARG;
     }
+    if (ka.nkp * ka.nseg != kb.nkp * kb.nseg || ka.nseg < 1 || ka.nseg > 8 || kb.nseg < 1 || kb.nseg > 8) {
+        set_error(FORGE_ERR_ARG, "tc_gemm: inconsistent K maps");
+        return FORGE_ERR_ARG;
+    }
     CUtensorMap ma, mb;
-    TcOperand a = A, bb = B;
-    a.cols = K;
-    bb.cols = K;
-    FORGE_TRY(tc_make_tmap(&ma, a, batch));
-    FORGE_TRY(tc_make_tmap(&mb, bb, batch));
+    FORGE_TRY(tc_make_tmap(&ma, A, batch));
+    FORGE_TRY(tc_make_tmap(&mb, B, batch));
     static bool attr_set = false;
     if (!attr_set) {
         FORGE_CUDA(cudaFuncSetAttribute(k_tc_gemm_tf32<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
         attr_set = true;
     }
     dim3 grd((unsigned)((A.rows + TC_BM - 1) / TC_BM), (unsigned)((B.rows + TC_BN - 1) / TC_BN), (unsigned)batch);
-    k_tc_gemm_tf32<EPI><<<grd, TC_THREADS, TC_SMEM, st>>>(ma, mb, A.rows, B.rows, K, epi, err);
+    k_tc_gemm_tf32<EPI><<<grd, TC_THREADS, TC_SMEM, st>>>(ma, mb, A.rows, B.rows, ka, kb, lower_div, epi, err);
     FORGE_LAUNCH_CHECK();
     return 0;
+}
+
+// Plain form: row-major A (M x K) and B (N x K), batch in the 3rd dimension.
+template <class EPI>
+int tc_gemm_tf32(cudaStream_t st, const TcOperand& A, const TcOperand& B, int64_t K, int64_t batch, const EPI& epi,
+                 int* err, int64_t lower_div = 0) {
+    TcOperand a = A, bb = B;
+    a.cols = K;
+    bb.cols = K;
+    a.nplanes = batch;
+    bb.nplanes = batch;
+    return tc_gemm_tf32_mapped(st, a, tc_kmap_plain(K), bb, tc_kmap_plain(K), batch, lower_div, epi, err);
 }
 
 }  // namespace forge

@@ -478,6 +478,9 @@ int eig_fp64(cudaStream_t st, EigArgs& g) {
     FORGE_CUDA(cudaMemsetAsync(g.cnt, 0, sizeof(unsigned) * 4 * batch, st));
     FORGE_TRY(tridiagonalize<double>(st, a, batch));
     FORGE_TRY(tridiag_eigvecs(st, g));
+    dim3 gz((unsigned)((n + 31) / 32), (unsigned)((iu + 31) / 32), (unsigned)batch);
+    k_z_to_x<<<gz, dim3(32, 8), 0, st>>>(g.Z, n, iu, g.X, g.ldx, g.strideX);
+    FORGE_LAUNCH_CHECK();
     prof_begin(ST_BACKTRANSFORM);
     FORGE_TRY(backtransform_fp64(st, g.A, g.lda, g.strideA, g.tau, n, g.X, g.ldx, g.strideX, iu, batch, g.G, g.T,
                                  g.Wb, g.W2b));
@@ -504,9 +507,6 @@ int tridiag_eigvecs(cudaStream_t st, EigArgs& g) {
     k_invit<<<gi, 64, 0, st>>>(g.d, g.e, n, iu, g.w, g.info, g.clus, g.Z, g.scr, g.pivs, g.scr_stride, g.fail);
     FORGE_LAUNCH_CHECK();
     prof_end(ST_INVIT, batch * 8.0 * (double)n * iu, 0.0);
-    dim3 gz((unsigned)((n + 31) / 32), (unsigned)((iu + 31) / 32), (unsigned)batch);
-    k_z_to_x<<<gz, dim3(32, 8), 0, st>>>(g.Z, n, iu, g.X, g.ldx, g.strideX);
-    FORGE_LAUNCH_CHECK();
     return 0;
 }
 

@@ -400,7 +400,10 @@ int tridiagonalize(cudaStream_t st, TrdArgs<T>& a, int64_t batch) {
         if (nrefl > 0 && p + w < n) {
             const double m2 = (double)(n - p - w);
             prof_begin(ST_HER2K);
-            FORGE_TRY(her2k_update<T>(st, a, p, nrefl, batch));
+            if (a.her2k)
+                FORGE_TRY(a.her2k(st, a, p, nrefl, batch, a.her2k_user));
+            else
+                FORGE_TRY(her2k_update<T>(st, a, p, nrefl, batch));
             prof_end(ST_HER2K, batch * m2 * m2 * (double)sizeof(typename CV<T>::type),
                      batch * 8.0 * m2 * m2 * (double)nrefl);  // lower half of 2*nrefl complex MACs
         }
@@ -409,5 +412,6 @@ int tridiagonalize(cudaStream_t st, TrdArgs<T>& a, int64_t batch) {
 }
 
 template int tridiagonalize<double>(cudaStream_t, TrdArgs<double>&, int64_t);
+template int tridiagonalize<float>(cudaStream_t, TrdArgs<float>&, int64_t);
 
 }  // namespace forge

@@ -42,6 +42,10 @@ struct TrdArgs {
     int64_t pstride;
     double* scal;       // batch x 16
     unsigned* cnt;      // batch x 4
+    // optional trailing-update override (the tensor-core rank-2k update of the mixed path):
+    // A(p+w:n, p+w:n) -= V W^H + W V^H for the panel [p, p+w)
+    int (*her2k)(cudaStream_t st, TrdArgs<T>& a, int64_t p, int64_t w, int64_t batch, void* user) = nullptr;
+    void* her2k_user = nullptr;
 };
 
 template <class T>

@@ -191,6 +191,23 @@ int forge_gpu_profile_read(forge_ctx* ctx, double* ms, int64_t* launches, double
 int forge_gpu_selftest_tc_gemm(int64_t M, int64_t N, int64_t K, int64_t batch, const float* A, const float* B,
                                float* D);
 
+/* Learned SCF warm start (no counterpart in the reference, which starts from the non-interacting
+ * guess or a checkpoint): an MLP din -> 128 -> 128 -> 128 -> dout (SiLU), BF16 weights, FP32
+ * accumulation and master weights, trained with Adam by hand-written kernels.  X: n x din,
+ * targets / outputs: n x dout, row-major fp32 host arrays.  Loss: sum_o wt_o (y_o - t_o)^2 / n. */
+typedef struct forge_mlp forge_mlp;
+int forge_gpu_mlp_create(int64_t din, int64_t dout, uint64_t seed, forge_mlp** mlp);
+int forge_gpu_mlp_destroy(forge_mlp* mlp);
+int64_t forge_gpu_mlp_num_params(forge_mlp* mlp);
+int forge_gpu_mlp_set_params(forge_mlp* mlp, const float* params);
+int forge_gpu_mlp_get_params(forge_mlp* mlp, float* params, float* params_bf16);
+int forge_gpu_mlp_set_loss_weights(forge_mlp* mlp, const float* wt);
+int forge_gpu_mlp_forward(forge_mlp* mlp, const float* X, int64_t n, float* Y);
+int forge_gpu_mlp_gradient(forge_mlp* mlp, const float* X, const float* targets, int64_t n, float* grad,
+                           float* loss);
+int forge_gpu_mlp_train(forge_mlp* mlp, const float* X, const float* targets, int64_t n, int64_t epochs,
+                        int64_t batch, double lr, uint64_t seed, float* last_loss);
+
 /* Synchronises the context's stream (for host timing). */
 int forge_gpu_synchronize(forge_ctx* ctx);
 
