@@ -51,7 +51,8 @@ class forge_iter_report(C.Structure):
 
 class forge_scf_options(C.Structure):
     _fields_ = [("itmax", C.c_int64), ("residual_tol", C.c_double), ("mixed_until", C.c_int64),
-                ("mixed_switch_tol", C.c_double), ("output_dir", C.c_char_p), ("statename", C.c_char_p)]
+                ("mixed_switch_tol", C.c_double), ("output_dir", C.c_char_p), ("statename", C.c_char_p),
+                ("nMomentaFlattened", C.c_void_p), ("g1", C.c_void_p), ("g12", C.c_void_p)]
 
 
 class forge_scf_result(C.Structure):
@@ -75,6 +76,7 @@ SIGNATURES = {
     "forge_gpu_zheevr_batch": [_P, _I, _P, _I, _P, _P],
     "forge_gpu_solve": [_P, _P, _P, _P, _P, _P],
     "forge_gpu_sort_energies": [_P, _P, _P, _P],
+    "forge_gpu_get_bands": [_P, _P],
     "forge_gpu_fermi": [_P, _D, _P, _P, _P, _P, _P],
     "forge_gpu_get_fock": [_P, _D, _I, _I, _P],
     "forge_gpu_energies": [_P, _P, _P, _P, _P, _P],
@@ -82,6 +84,7 @@ SIGNATURES = {
     "forge_gpu_mix_potential": [_P, _D, _P, _P],
     "forge_gpu_plain_guess": [_P, _P],
     "forge_gpu_prepare_state": [_P, _P],
+    "forge_gpu_field_guess": [_P, _P, _P, _P],
     "forge_gpu_scf_iteration": [_P, _P, _P],
     "forge_gpu_set_precision": [_P, _I],
     "forge_gpu_get_setup": [_P, _P],
@@ -103,6 +106,7 @@ SIGNATURES = {
     "forge_host_geometry": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "forge_host_run_scf": [_P, _P, _P, _P, _P],
     "forge_host_parameters_string": [_P, C.c_char_p, C.c_char_p, _I],
+    "forge_host_plot_bands": [_P, _P, _D, _P, _P, _P, C.c_char_p],
 }
 
 _LIB = None
@@ -222,6 +226,16 @@ def build_geometry(setup: Setup) -> Geometry:
         _ptr(out.nMomentaFlattened), _ptr(out.nC2pairs), _ptr(out.nC3pairs), _ptr(counts)))
     out.c2_count, out.c3_count = int(counts[0]), int(counts[1])
     return out
+
+
+def plot_bands(setup: Setup, geometry: Geometry, Bands: np.ndarray, FermiEnergy: float, path: str) -> None:
+    """PlotBands (TightBinding.f90:275-369) through forge_host_plot_bands."""
+    s = setup.to_struct()
+    B = _f(Bands, np.float64)
+    _check(load_library().forge_host_plot_bands(C.byref(s), _ptr(B), FermiEnergy,
+                                                 _ptr(_f(geometry.nMomentaFlattened, np.int64)),
+                                                 _ptr(np.ascontiguousarray(geometry.g1)),
+                                                 _ptr(np.ascontiguousarray(geometry.g12)), path.encode()))
 
 
 def parameters_string(setup: Setup, statename: str = "SSS") -> str:
@@ -387,8 +401,12 @@ class HartreeFock:
     def RunScf(self, itmax: int, residual_tol: float = 0.0, mixed_until: int = 0, mixed_switch_tol: float = 0.0,
                zFock_init=None, output_dir: Optional[str] = None, statename: str = "SSS"):
         """Main.f90:236-679 via forge_host_run_scf: (result dict, list of per-iteration reports)."""
+        g = self.geometry
+        self._flat = _f(g.nMomentaFlattened, np.int64)
+        self._g = (np.ascontiguousarray(g.g1, dtype=np.float64), np.ascontiguousarray(g.g12, dtype=np.float64))
         opts = forge_scf_options(itmax, residual_tol, mixed_until, mixed_switch_tol,
-                                 None if output_dir is None else output_dir.encode(), statename.encode())
+                                 None if output_dir is None else output_dir.encode(), statename.encode(),
+                                 _ptr(self._flat), _ptr(self._g[0]), _ptr(self._g[1]))
         res = forge_scf_result()
         reps = (forge_iter_report * max(1, itmax))()
         P0 = None if zFock_init is None else _f(zFock_init, np.complex128)

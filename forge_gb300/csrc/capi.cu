@@ -1,6 +1,7 @@
 // C-ABI entry points (include/forge_gpu.h): one per reference routine of the SCF
 // path, plus a fused device-resident iteration.  Host code here is compiled with
 // -ffp-contract=off so that the k.R phases follow the reference's unfused dot product.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -666,6 +667,22 @@ int forge_gpu_solve(forge_ctx* x, const double* Potential, const double* zFock, 
     return info;
 }
 
+int forge_gpu_get_bands(forge_ctx* x, double* Bands) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!x->have_solve || !Bands) {
+        set_error(FORGE_ERR_STATE, "get_bands needs a solve first");
+        return FORGE_ERR_STATE;
+    }
+    const int64_t iu = c.nUpper, Nk = c.Nk, numb = c.numb;
+    std::vector<double> w((size_t)Nk * iu);
+    FORGE_CUDA(cudaMemcpyAsync(w.data(), x->w.ptr, w.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    for (int64_t k = 0; k < Nk; ++k)
+        for (int64_t b = 0; b < numb; ++b) Bands[b + k * numb] = w[k * iu + c.nLower - 1 + b];
+    return 0;
+}
+
 int forge_gpu_sort_energies(forge_ctx* x, double* SortedEnergies, int64_t* nSortedMomenta, int64_t* nSortedIndex) {
     FORGE_TRY(check_ctx(x));
     Context& c = x->c;
@@ -828,6 +845,60 @@ int forge_gpu_plain_guess(forge_ctx* x, double* Energies) {
     // Main.f90:255: nFermiLevel without the numS factor (numS = 1 here)
     FORGE_TRY(sort_device(x, c.s.nfilling));
     FORGE_TRY(project_fused(x));
+    FORGE_CUDA(cudaMemcpyAsync(c.P.ptr, x->Pn.ptr, 4 * NN * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream));
+    x->have_pnew = false;
+    FORGE_TRY(prepare_state_device(x, Energies));
+    return info;
+}
+
+int forge_gpu_field_guess(forge_ctx* x, const double* zFock, double* Energies, double* residuals) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!zFock || !residuals) {
+        set_error(FORGE_ERR_ARG, "field_guess: null argument");
+        return FORGE_ERR_ARG;
+    }
+    if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
+    const int64_t N = c.N;
+    const size_t NN = (size_t)N * N;
+    // predicted field: P_pred and V_pred = 2 alphaH LR dn + U dn from its diagonal
+    FORGE_TRY(upload_state(x, nullptr, zFock));
+    FORGE_TRY(scf_density(c, c.P.as<double2>(), c.dens.as<double>()));
+    FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), c.P.as<double2>(), c.dens.as<double>(),
+                               c.dens.as<double>(), x->y.as<double>(), x->work.as<double>(), x->sc.as<ScfScalars>()));
+    FORGE_TRY(scf_potential(c, x->y.as<double>(), c.dens.as<double>(), c.V.as<double>()));
+    std::vector<double> Vpred(N), V1(N);
+    FORGE_CUDA(cudaMemcpyAsync(Vpred.data(), c.V.ptr, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    // one diagonalisation in that field (the cost of the plain guess)
+    int info = 0;
+    FORGE_TRY(solve_device(x, &info, false));
+    FORGE_TRY(sort_device(x, c.s.nfilling));
+    FORGE_TRY(project_fused(x));  // P_1 in Pn; c.bulk is all zeros afterwards
+    // residuals of the predicted field and of the zero field against the field of P_1
+    FORGE_TRY(scf_density(c, x->Pn.as<double2>(), x->dens_new.as<double>()));
+    FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(),
+                               x->dens_new.as<double>(), x->y.as<double>(), x->work.as<double>(),
+                               x->sc.as<ScfScalars>()));
+    ScfScalars h;
+    FORGE_TRY(read_scalars(x, &h));
+    const double fock_ws = h.forms[5];
+    FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.bulk.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(),
+                               x->dens_new.as<double>(), x->y.as<double>(), x->work.as<double>(),
+                               x->sc.as<ScfScalars>()));
+    FORGE_TRY(read_scalars(x, &h));
+    const double fock_zero = h.forms[5];
+    // V of P_1 (y holds LR dn_b from the last forms pass)
+    FORGE_TRY(scf_potential(c, x->y.as<double>() + N, x->dens_new.as<double>(), c.V.as<double>()));
+    FORGE_CUDA(cudaMemcpyAsync(V1.data(), c.V.ptr, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    double dv_ws = 0.0, dv_zero = 0.0;
+    for (int64_t i = 0; i < N; ++i) {
+        dv_ws = std::max(dv_ws, std::fabs(V1[i] - Vpred[i]));
+        dv_zero = std::max(dv_zero, std::fabs(V1[i]));
+    }
+    residuals[0] = std::max(dv_ws, fock_ws);
+    residuals[1] = std::max(dv_zero, fock_zero);
+    // the state becomes P_1 (Main.f90:281-346 with the predicted field in place of zero)
     FORGE_CUDA(cudaMemcpyAsync(c.P.ptr, x->Pn.ptr, 4 * NN * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream));
     x->have_pnew = false;
     FORGE_TRY(prepare_state_device(x, Energies));

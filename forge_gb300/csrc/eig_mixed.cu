@@ -63,7 +63,7 @@ void carve(MixedWs& w, Carve& c) {
     w.Kp = (n + 31) / 32 * 32;
     w.nblk = (n + TRD_TILE - 1) / TRD_TILE;
     w.nrb = (n + 255) / 256;
-    w.pstride = 2 * ((n + TRD_ROWS - 1) / TRD_ROWS) + 2;
+    w.pstride = 2 * ((n + 31) / 32) + 2;  // per-CTA partials of trd_col / trd_finish
     w.A32 = c.take<float2>(B * n * n);
     w.W = c.take<float2>(B * n * TRD_NB);
     w.Yrow = c.take<float2>(B * w.nblk * n);

@@ -249,6 +249,43 @@ int forge_host_geometry(const forge_setup* s, const int64_t* RotateLayers, doubl
     return 0;
 }
 
+int forge_host_plot_bands(const forge_setup* s, const double* Bands, double FermiEnergy,
+                          const int64_t* nMomentaFlattened, const double* g1, const double* g12, const char* path) {
+    if (!s || !Bands || !nMomentaFlattened || !g1 || !g12 || !path) return FORGE_ERR_ARG;
+    FILE* f = std::fopen(path, "w");
+    if (!f) return FORGE_ERR_ARG;
+    // PlotBands (TightBinding.f90:275-369): K - Gamma - M - K path through the k-grid points
+    const int64_t numk = s->numk, numb = s->numb, p = 0;
+    const double vK1x = (g1[0] + g12[0]) / 3.0, vK1y = (g1[1] + g12[1]) / 3.0;
+    const double vMx = (g1[0] + g12[0]) / 2.0, vMy = (g1[1] + g12[1]) / 2.0;
+    const double aKG = std::sqrt(vK1x * vK1x + vK1y * vK1y);
+    const double aGM = std::sqrt((vMx - g12[0]) * (vMx - g12[0]) + (vMy - g12[1]) * (vMy - g12[1]));
+    const double aMK = std::sqrt((vK1x - vMx) * (vK1x - vMx) + (vK1y - vMy) * (vK1y - vMy));
+    const double aT = 3 * aKG + aGM + aMK;
+    auto mod = [](int64_t a, int64_t b) { return ((a % b) + b) % b; };
+    auto line = [&](double x, int64_t ivk1, int64_t ivk2) {
+        const int64_t k = nMomentaFlattened[ivk1 + ivk2 * numk] - 1;  // 1-based flat index
+        std::fprintf(f, "%16.8f   ", x);
+        for (int64_t i = 0; i < numb; ++i) std::fprintf(f, "%16.8f   ", Bands[i + k * numb] - FermiEnergy);
+        std::fprintf(f, "\n");
+    };
+    const double n3 = (double)(numk / 3), n6 = (double)(numk / 6), n2 = (double)(numk / 2);
+    for (int64_t ivk = 0; ivk <= numk / 3 - 1; ++ivk)
+        line(ivk * aKG / n3 / aT, mod(2 * numk / 3 + ivk, numk), mod(2 * numk / 3 - 2 * ivk + p * numk / 2, numk));
+    line(aKG / aT, 0, p * numk / 2);
+    for (int64_t ivk = 1; ivk <= numk / 3; ++ivk)
+        line(aKG / aT + aKG * ivk / n3 / aT, mod(ivk, numk), mod(numk - 2 * ivk + p * numk / 2, numk));
+    for (int64_t ivk = 1; ivk <= numk / 6; ++ivk)
+        line(2 * aKG / aT + aMK * ivk / n6 / aT, mod(numk / 3 + ivk, numk), mod(numk / 3 + ivk + p * numk / 2, numk));
+    for (int64_t ivk = 1; ivk <= numk / 2 - 1; ++ivk)
+        line((2 * aKG + aMK) / aT + aGM * ivk / n2 / aT, mod(numk / 2 - ivk, numk),
+             mod(numk / 2 + ivk + p * numk / 2, numk));
+    for (int64_t ivk = 0; ivk <= numk / 3; ++ivk)
+        line((2 * aKG + aMK + aGM) / aT + ivk * aKG / n3 / aT, mod(ivk, numk), mod(ivk + p * numk / 2, numk));
+    std::fclose(f);
+    return 0;
+}
+
 int forge_host_parameters_string(const forge_setup* s, const char* statename, char* buf, int64_t buflen) {
     if (!s || !buf || buflen < 8) return FORGE_ERR_ARG;
     // Main.f90:180-183
@@ -329,6 +366,20 @@ int forge_host_run_scf(forge_ctx* ctx, const forge_scf_options* opts, const doub
         if (fe)  // Main.f90:625-631
             std::fprintf(fe, "%5.1f   %24.9f   %24.9f   %24.9f   %24.9f   %24.9f   \n", (double)it, r.TotalEnergyIn,
                          2.0 * r.KineticEnergyIn, 2.0 * r.FockEnergyIn, r.HartreeEnergyIn, r.HubbardEnergyIn);
+        if (fe && opts->nMomentaFlattened && opts->g1 && opts->g12) {
+            // output/Bands-nspin1<parameters> (Main.f90:601-610), rewritten every iteration
+            forge_setup s;
+            char params[256];
+            forge_gpu_get_setup(ctx, &s);
+            forge_host_parameters_string(&s, opts->statename, params, sizeof(params));
+            std::vector<double> bands((size_t)s.numb * s.numk * s.numk);
+            if (forge_gpu_get_bands(ctx, bands.data()) == 0) {
+                std::string d(opts->output_dir);
+                if (!d.empty() && d.back() != '/') d += '/';
+                forge_host_plot_bands(&s, bands.data(), r.FermiEnergy, opts->nMomentaFlattened, opts->g1, opts->g12,
+                                      (d + "Bands-nspin1" + params).c_str());
+            }
+        }
         result->TotalEnergy = r.TotalEnergy;
         if (opts->residual_tol > 0.0 && res < opts->residual_tol && !mixed) {
             result->converged = 1;

@@ -532,7 +532,7 @@ void carve(EigArgs& g, Carve& c) {
     const int64_t nrb = (n + 255) / 256;
     g.ystride = nblk * n;
     g.sstride = nrb * 2 * TRD_NB;
-    g.pstride = 2 * ((n + TRD_ROWS - 1) / TRD_ROWS) + 2;
+    g.pstride = 2 * ((n + 31) / 32) + 2;  // per-CTA partials of trd_col / trd_finish
     g.scr_stride = iu;
     g.d = c.take<double>(B * n);
     g.e = c.take<double>(B * n);

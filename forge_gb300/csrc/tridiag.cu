@@ -159,23 +159,25 @@ __global__ void __launch_bounds__(256) k_trd_hemv(TrdArgs<T> a, int64_t p, int i
         __syncthreads();
         const int tr = threadIdx.x & 63, tg = threadIdx.x >> 6;
         const int64_t row = R0 + tr;
+        const bool diag = (bi == bj);
+        // all 16 loads of this thread are issued before any arithmetic
+        V av[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int64_t c = C0 + tg * 16 + q;
+            av[q] = (row < n && c < n && (!diag || c <= row)) ? A[row + c * lda] : vzero<V>();
+        }
         V racc = vzero<V>();
         V cacc[16];
+        const V vrow = vr[tr];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) cacc[q] = vzero<V>();
-        const bool diag = (bi == bj);
-        if (row < n) {
-            const V vrow = vr[tr];
-#pragma unroll 4
-            for (int q = 0; q < 16; ++q) {
-                const int64_t c = C0 + tg * 16 + q;
-                if (c < n && (!diag || c <= row)) {
-                    V av = A[row + c * lda];
-                    if (c == row) av.y = 0;
-                    racc = vadd(racc, vmul(av, vc[tg * 16 + q]));
-                    if (c != row) cacc[q] = vadd(cacc[q], vcjmul(av, vrow));
-                }
-            }
+        for (int q = 0; q < 16; ++q) {
+            const int64_t c = C0 + tg * 16 + q;
+            V x = av[q];
+            const bool on_diag = diag && (c == row);
+            if (on_diag) x.y = 0;
+            racc = vadd(racc, vmul(x, vc[tg * 16 + q]));
+            cacc[q] = on_diag ? vzero<V>() : vcjmul(x, vrow);
         }
         rsum[tg][tr] = racc;
         const int lane = threadIdx.x & 31, half = (threadIdx.x >> 5) & 1;
@@ -258,16 +260,25 @@ __global__ void __launch_bounds__(TRD_ROWS) k_trd_finish(TrdArgs<T> a, int64_t p
         s1[threadIdx.x] = x1;
         s2[threadIdx.x] = x2;
     }
-    __syncthreads();
-    const int64_t r = c0 + (int64_t)blockIdx.x * TRD_ROWS + threadIdx.x;
-    double dre = 0.0, dim = 0.0;
+    // 32 rows per CTA, 8 threads per row share the sum over the Yrow / Ycol partial slots
+    __shared__ V ysl[8][33];
+    const int rr = threadIdx.x & 31, sl = threadIdx.x >> 5;
+    const int64_t r = c0 + (int64_t)blockIdx.x * 32 + rr;
     if (r < n) {
         const int64_t B = (r - c0) / TRD_TILE;
         const V* Yrow = a.Yrow + b * a.ystride;
         const V* Ycol = a.Ycol + b * a.ystride;
         V y = vzero<V>();
-        for (int64_t q = 0; q <= B; ++q) y = vadd(y, Yrow[q * n + r]);
-        for (int64_t q = B; q < nb2; ++q) y = vadd(y, Ycol[q * n + r]);
+        for (int64_t q = sl; q <= B; q += 8) y = vadd(y, Yrow[q * n + r]);
+        for (int64_t q = B + sl; q < nb2; q += 8) y = vadd(y, Ycol[q * n + r]);
+        ysl[sl][rr] = y;
+    }
+    __syncthreads();
+    double dre = 0.0, dim = 0.0;
+    if (sl == 0 && r < n) {
+        V y = vzero<V>();
+#pragma unroll
+        for (int q = 0; q < 8; ++q) y = vadd(y, ysl[q][rr]);
         for (int l = 0; l < ii; ++l) {
             y = vsub(y, vmul(A[r + (p + l) * lda], s1[l]));
             y = vsub(y, vmul(W[r + l * n], s2[l]));
@@ -389,9 +400,10 @@ int tridiagonalize(cudaStream_t st, TrdArgs<T>& a, int64_t batch) {
             FORGE_LAUNCH_CHECK();
             // algorithmic traffic: the trailing lower triangle read once
             prof_end(ST_HEMV, batch * 0.5 * (double)n2 * (double)(n2 + 1) * esz, batch * 8.0 * (double)n2 * n2);
+            dim3 gf((unsigned)((n2 + 31) / 32), (unsigned)batch);
             dim3 gc((unsigned)((n2 + TRD_ROWS - 1) / TRD_ROWS), (unsigned)batch);
             prof_begin(ST_TRD_FINISH);
-            k_trd_finish<T><<<gc, TRD_ROWS, 0, st>>>(a, p, ii, col, nb2, ii > 0 ? nrb : 0);
+            k_trd_finish<T><<<gf, TRD_ROWS, 0, st>>>(a, p, ii, col, nb2, ii > 0 ? nrb : 0);
             FORGE_LAUNCH_CHECK();
             k_trd_fix<T><<<gc, TRD_ROWS, 0, st>>>(a, ii, col);
             FORGE_LAUNCH_CHECK();

@@ -126,6 +126,9 @@ int forge_gpu_zheevr_batch(forge_ctx* ctx, int64_t nb, const double* A, int64_t 
 int forge_gpu_solve(forge_ctx* ctx, const double* Potential, const double* zFock, double* Bands,
                     double* zEigenvectors, double* zFockBulk);
 
+/* Bands (numb x Nk) of the last Solve or SCF iteration (HartreeFock.f90:444-446). */
+int forge_gpu_get_bands(forge_ctx* ctx, double* Bands);
+
 /* SortEnergies_1Spin (HartreeFock.f90:885-925) of the last Solve: SortedEnergies (numb*Nk),
  * nSortedMomenta (numb*Nk x 2), nSortedIndex (numb*Nk, the reference's flattened index
  * icount = (band-1)*Nk + k, 1-based); any output may be NULL. */
@@ -158,6 +161,14 @@ int forge_gpu_mix_potential(forge_ctx* ctx, double Step, double* DensityConverge
 /* Initial guess without a checkpoint (Main.f90:236-346, nRead=0): non-interacting Solve,
  * sort, Fermi, GetFock, energies and potential.  Energies[4] as in optimal_step. */
 int forge_gpu_plain_guess(forge_ctx* ctx, double* Energies);
+
+/* Initial guess from a predicted mean field (no counterpart in the reference): zFock holds the
+ * predicted density matrix (e.g. a learned warm start on short bonds plus site densities); its
+ * field is diagonalised once like the plain guess, and the resulting density matrix becomes the
+ * state.  residuals[0] = residual of the predicted field, residuals[1] = residual of the zero
+ * field (the plain guess), both against the field of the new state; Energies[4] as in
+ * forge_gpu_optimal_step. */
+int forge_gpu_field_guess(forge_ctx* ctx, const double* zFock, double* Energies, double* residuals);
 
 /* After forge_gpu_set_state: energies and potential of the loaded state (Main.f90:290-346). */
 int forge_gpu_prepare_state(forge_ctx* ctx, double* Energies);

@@ -35,8 +35,11 @@ typedef struct forge_scf_options {
     double residual_tol;        /* > 0: stop once the mean-field residual is below it (eV) */
     int64_t mixed_until;        /* iterations run with FORGE_PREC_MIXED before switching to FP64 (0 = never) */
     double mixed_switch_tol;    /* > 0: switch to FP64 once the residual is below this (eV) */
-    const char* output_dir;     /* NULL: no Energy / Convergence files */
+    const char* output_dir;     /* NULL: no Energy / Convergence / Bands files */
     const char* statename;      /* label of the solution (Setup.f90:15), NULL = "SSS" */
+    const int64_t* nMomentaFlattened; /* with g1, g12: enables the Bands file (Main.f90:601-610) */
+    const double* g1;
+    const double* g12;
 } forge_scf_options;
 
 typedef struct forge_scf_result {
@@ -54,6 +57,11 @@ typedef struct forge_scf_result {
  * iteration (capacity opts->itmax). */
 int forge_host_run_scf(forge_ctx* ctx, const forge_scf_options* opts, const double* zFock_init,
                        forge_scf_result* result, forge_iter_report* reports);
+
+/* PlotBands (TightBinding.f90:275-369): writes Bands(numb, Nk) - FermiEnergy along the
+ * K - Gamma - M - K path of k-grid points to the file `path` (the reference's unit 99). */
+int forge_host_plot_bands(const forge_setup* s, const double* Bands, double FermiEnergy,
+                          const int64_t* nMomentaFlattened, const double* g1, const double* g12, const char* path);
 
 /* The parameter string of Main.f90:180-183 used in output file names. */
 int forge_host_parameters_string(const forge_setup* s, const char* statename, char* buf, int64_t buflen);

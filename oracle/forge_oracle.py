@@ -950,3 +950,35 @@ def order_parameters(s: Setup, g: Geometry, P) -> dict:
     c3n = float(np.linalg.norm(P0 - P0[np.ix_(c3, c3)])) if np.all(c3 >= 0) else float("nan")
     return dict(layer_polarization=float(layer), sublattice_polarization=float(sub), c2t_breaking=c2t,
                 c3_breaking=c3n)
+
+
+def plot_bands_lines(s: Setup, g: Geometry, bands, EF: float):
+    """PlotBands (TightBinding.f90:275-369) as a list of rows [x, Bands(1..numb) - EF] (p = 0)."""
+    numk, numb, p = s.numk, s.numb, 0
+    g1, g12 = g.g1, g.g12
+    vK1x, vK1y = (g1[0] + g12[0]) / 3.0, (g1[1] + g12[1]) / 3.0
+    vMx, vMy = (g1[0] + g12[0]) / 2.0, (g1[1] + g12[1]) / 2.0
+    aKG = math.sqrt(vK1x ** 2 + vK1y ** 2)
+    aGM = math.sqrt((vMx - g12[0]) ** 2 + (vMy - g12[1]) ** 2)
+    aMK = math.sqrt((vK1x - vMx) ** 2 + (vK1y - vMy) ** 2)
+    aT = 3 * aKG + aGM + aMK
+    n3, n6, n2 = float(numk // 3), float(numk // 6), float(numk // 2)
+    rows = []
+
+    def row(x, i1, i2):
+        k = g.kflat[i1, i2] - 1
+        rows.append([x] + [bands[b, k] - EF for b in range(numb)])
+
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for ivk in range(0, numk // 3):
+            row(np.float64(ivk) * aKG / n3 / aT, (2 * numk // 3 + ivk) % numk, (2 * numk // 3 - 2 * ivk + p * numk // 2) % numk)
+        row(aKG / aT, 0, p * numk // 2)
+        for ivk in range(1, numk // 3 + 1):
+            row(aKG / aT + aKG * ivk / n3 / aT, ivk % numk, (numk - 2 * ivk + p * numk // 2) % numk)
+        for ivk in range(1, numk // 6 + 1):
+            row(2 * aKG / aT + aMK * ivk / n6 / aT, (numk // 3 + ivk) % numk, (numk // 3 + ivk + p * numk // 2) % numk)
+        for ivk in range(1, numk // 2):
+            row((2 * aKG + aMK) / aT + aGM * ivk / n2 / aT, (numk // 2 - ivk) % numk, (numk // 2 + ivk + p * numk // 2) % numk)
+        for ivk in range(0, numk // 3 + 1):
+            row((2 * aKG + aMK + aGM) / aT + np.float64(ivk) * aKG / n3 / aT, ivk % numk, (ivk + p * numk // 2) % numk)
+    return rows

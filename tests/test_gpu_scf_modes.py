@@ -1,0 +1,45 @@
+"""SCF in the fast configuration (mixed-precision iterations, FP64 finish) reaches the same
+converged state as the FP64 oracle; the tensor-core projector agrees with the FP64 one."""
+import numpy as np
+import pytest
+
+from oracle import forge_oracle as fo
+
+pytestmark = pytest.mark.gpu
+
+
+def test_fused_projector_mixed_vs_fp64(lib):
+    import forge_gb300 as fg
+    S = fg.Setup(ntheta=4, numk=3, nfilling=2.0)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with fg.HartreeFock(S) as hf:
+            hf.LongRangeInteraction(copy_out=False)
+            hf.set_precision(prec)
+            E, info = hf.PlainGuess()
+            P, dens, V = hf.GetState()
+            out[prec] = (P, E)
+    Pd, Pm = out["fp64"][0], out["mixed"][0]
+    assert np.max(np.abs(Pd - Pm)) <= 2e-4
+    assert abs(out["fp64"][1][0] - out["mixed"][1][0]) / S.to_struct().ndim <= 1e-4
+
+
+@pytest.mark.parametrize("m,numk,nu", [(2, 3, 2.0), (3, 3, 0.0)])
+def test_fast_scf_converges_to_oracle_fixed_point(lib, m, numk, nu):
+    import forge_gb300 as fg
+    # P responds to the mean field through 1/gap, so both sides converge to 1e-11 eV for a 1e-8 P check
+    so = fo.Setup(ntheta=m, numk=numk, nfilling=nu)
+    ref = fo.run_scf(so, itmax=400, residual_tol=1e-11)
+    assert ref["logs"][-1].residual < 1e-11
+    S = fg.Setup(ntheta=m, numk=numk, nfilling=nu)
+    with fg.HartreeFock(S) as hf:
+        hf.LongRangeInteraction(copy_out=False)
+        res, reps = hf.RunScf(itmax=400, residual_tol=1e-11, mixed_switch_tol=1e-4)
+        P, dens, V = hf.GetState()
+    assert res["converged"]
+    # the fast run used mixed precision first
+    assert len(reps) >= 2
+    P = np.moveaxis(P, 2, 0)
+    assert np.max(np.abs(P - ref["P"])) <= 1e-8
+    assert abs(res["TotalEnergy"] - ref["Etot"]) / so.ndim <= 1e-7
+    assert np.max(np.abs(V - ref["V"])) <= 1e-7

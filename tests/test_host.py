@@ -74,3 +74,20 @@ def test_init_without_gpu_reports_error(lib):
     import forge_gb300 as fg
     with pytest.raises(fg.ForgeError):
         fg.HartreeFock(fg.Setup(ntheta=1, numk=2))
+
+
+@pytest.mark.parametrize("numk", [6, 12])
+def test_plot_bands_matches_oracle(lib, tmp_path, numk):
+    import forge_gb300 as fg
+    S = fg.Setup(ntheta=2, numk=numk)
+    g = fg.build_geometry(S)
+    so = fo.Setup(ntheta=2, numk=numk)
+    go = fo.build_geometry(so)
+    rng = np.random.default_rng(numk)
+    bands = rng.standard_normal((so.numb, so.Nk))
+    path = str(tmp_path / "bands.dat")
+    fg.api.plot_bands(S, g, bands, 0.25, path)
+    rows = [list(map(float, l.split())) for l in open(path) if l.strip()]
+    ref = fo.plot_bands_lines(so, go, bands, 0.25)
+    assert len(rows) == len(ref)
+    assert np.max(np.abs(np.array(rows) - np.round(np.array(ref), 8))) <= 1e-8
