@@ -77,6 +77,10 @@ SIGNATURES = {
     "forge_gpu_solve": [_P, _P, _P, _P, _P, _P],
     "forge_gpu_sort_energies": [_P, _P, _P, _P],
     "forge_gpu_get_bands": [_P, _P],
+    "forge_gpu_set_kshard": [_P, _I, _I],
+    "forge_gpu_set_bands": [_P, _P],
+    "forge_gpu_project_local": [_P, _P],
+    "forge_gpu_set_pnew": [_P, _P],
     "forge_gpu_fermi": [_P, _D, _P, _P, _P, _P, _P],
     "forge_gpu_get_fock": [_P, _D, _I, _I, _P],
     "forge_gpu_energies": [_P, _P, _P, _P, _P, _P],

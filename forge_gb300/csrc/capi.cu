@@ -81,6 +81,7 @@ struct forge_ctx {
     DevBuf states, sorted_e, sorted_idx, sc, work, y, dens_new, w;
     DevBuf projws, tcerr;  // tensor-core projector staging and its error flag
     int64_t eig_batch = 0;
+    int64_t k_begin = 0, k_end = 0;  // local k range (k_end = 0: all k)
     bool have_solve = false, have_sort = false, have_pnew = false, have_state = false, bulk_is_fused = false;
     std::vector<int64_t> h_sorted_idx;
     std::vector<double2> h_bph;
@@ -198,8 +199,10 @@ int solve_device(forge_ctx* x, int* info, bool with_projector = true) {
                                c.stream));
     FORGE_CUDA(cudaStreamSynchronize(c.stream));
     if (x->tcerr.ptr) FORGE_CUDA(cudaMemsetAsync(x->tcerr.ptr, 0, sizeof(int), c.stream));
-    for (int64_t k0 = 0; k0 < Nk; k0 += B) {
-        const int64_t nb = (Nk - k0 < B) ? Nk - k0 : B;
+    // local k range of this rank (all k unless forge_gpu_set_kshard narrowed it)
+    const int64_t kb = x->k_begin, ke = (x->k_end > 0) ? x->k_end : Nk;
+    for (int64_t k0 = kb; k0 < ke; k0 += B) {
+        const int64_t nb = (ke - k0 < B) ? ke - k0 : B;
         FORGE_TRY(launch_assemble(c, c.V.as<double>(), c.P.as<double2>(), k0, nb, c.H.as<double2>()));
         FORGE_TRY(eig_batch_run(x, k0, nb, info));
         if (with_projector)
@@ -232,14 +235,18 @@ int project_fused(forge_ctx* x) {
     FORGE_TRY(x->Pn.ensure(4 * NN * sizeof(double2)));
     FORGE_CUDA(cudaMemsetAsync(x->Pn.ptr, 0, 4 * NN * sizeof(double2), c.stream));
     if (x->tcerr.ptr) FORGE_CUDA(cudaMemsetAsync(x->tcerr.ptr, 0, sizeof(int), c.stream));
-    for (int64_t k = 0; k < Nk; ++k)
+    const int64_t kb = x->k_begin, ke = (x->k_end > 0) ? x->k_end : Nk;
+    for (int64_t k = kb; k < ke; ++k)
         FORGE_TRY(project_k(x, k, c.nLower - 1 + fk[k], &x->h_bph[k * 4], x->Pn.as<double2>()));
-    if (npart > 0) {
-        // partially occupied states (complex weight zdeg in reference mode): full N x N products
-        FORGE_CUDA(cudaMemcpyAsync(x->states.ptr, st.data() + (nocc - npart), npart * sizeof(WinState),
-                                   cudaMemcpyHostToDevice, c.stream));
-        FORGE_TRY(window_projector_fp64(c.stream, x->states.as<WinState>(), npart, c.X.as<double2>(), c.N,
-                                        c.N * c.nUpper, c.N, x->Pn.as<double2>()));
+    // partially occupied states of local k points (complex weight zdeg in reference mode)
+    std::vector<WinState> part;
+    for (int64_t q = nocc - npart; q < nocc; ++q)
+        if (st[q].k >= kb && st[q].k < ke) part.push_back(st[q]);
+    if (!part.empty()) {
+        FORGE_CUDA(cudaMemcpyAsync(x->states.ptr, part.data(), part.size() * sizeof(WinState), cudaMemcpyHostToDevice,
+                                   c.stream));
+        FORGE_TRY(window_projector_fp64(c.stream, x->states.as<WinState>(), (int64_t)part.size(), c.X.as<double2>(),
+                                        c.N, c.N * c.nUpper, c.N, x->Pn.as<double2>()));
     }
     FORGE_CUDA(cudaMemsetAsync(c.bulk.ptr, 0, 4 * NN * sizeof(double2), c.stream));
     FORGE_TRY(scf_combine(c, x->Pn.as<double2>(), c.bulk.as<double2>()));
@@ -665,6 +672,63 @@ int forge_gpu_solve(forge_ctx* x, const double* Potential, const double* zFock, 
                                    c.stream));
     FORGE_CUDA(cudaStreamSynchronize(c.stream));
     return info;
+}
+
+int forge_gpu_set_kshard(forge_ctx* x, int64_t k_begin, int64_t k_end) {
+    FORGE_TRY(check_ctx(x));
+    if (k_begin < 0 || k_end > x->c.Nk || k_begin >= k_end) {
+        set_error(FORGE_ERR_ARG, "set_kshard: bad range [%lld, %lld)", (long long)k_begin, (long long)k_end);
+        return FORGE_ERR_ARG;
+    }
+    x->k_begin = k_begin;
+    x->k_end = k_end;
+    return 0;
+}
+
+int forge_gpu_set_bands(forge_ctx* x, const double* Bands) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!x->have_solve || !Bands) {
+        set_error(FORGE_ERR_STATE, "set_bands needs a solve first");
+        return FORGE_ERR_STATE;
+    }
+    const int64_t iu = c.nUpper, numb = c.numb;
+    for (int64_t k = 0; k < c.Nk; ++k)
+        FORGE_CUDA(cudaMemcpyAsync(x->w.as<double>() + k * iu + c.nLower - 1, Bands + k * numb,
+                                   numb * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    x->have_sort = false;
+    return 0;
+}
+
+int forge_gpu_project_local(forge_ctx* x, double* zFock) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!x->have_sort) {
+        set_error(FORGE_ERR_STATE, "project_local needs sort_energies / fermi first");
+        return FORGE_ERR_STATE;
+    }
+    FORGE_TRY(project_fused(x));
+    if (zFock)
+        FORGE_CUDA(cudaMemcpyAsync(zFock, x->Pn.ptr, 4 * (size_t)c.N * c.N * sizeof(double2), cudaMemcpyDeviceToHost,
+                                   c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+int forge_gpu_set_pnew(forge_ctx* x, const double* zFock) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!zFock) {
+        set_error(FORGE_ERR_ARG, "set_pnew: null zFock");
+        return FORGE_ERR_ARG;
+    }
+    const size_t NN = (size_t)c.N * c.N;
+    FORGE_TRY(x->Pn.ensure(4 * NN * sizeof(double2)));
+    FORGE_CUDA(cudaMemcpyAsync(x->Pn.ptr, zFock, 4 * NN * sizeof(double2), cudaMemcpyHostToDevice, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    x->have_pnew = true;
+    return 0;
 }
 
 int forge_gpu_get_bands(forge_ctx* x, double* Bands) {

@@ -32,7 +32,7 @@ from .api import ForgeError, Geometry, HartreeFock, Setup, _check, _ptr, load_li
 
 BOND_CUTOFF = 1.6           # lattice constants a (2.46 A): up to 4th in-plane neighbours, AA-like interlayer
 DENS_SCALE = 100.0          # network units of the site target
-SITE_IN, BOND_IN = 12, 20
+SITE_IN, BOND_IN = 12, 18
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "warmstart_weights.npz")
 
 

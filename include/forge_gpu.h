@@ -129,6 +129,17 @@ int forge_gpu_solve(forge_ctx* ctx, const double* Potential, const double* zFock
 /* Bands (numb x Nk) of the last Solve or SCF iteration (HartreeFock.f90:444-446). */
 int forge_gpu_get_bands(forge_ctx* ctx, double* Bands);
 
+/* k-point sharding across ranks (the reference's OpenMP k loop, HartreeFock.f90:424-478, split
+ * over GPUs).  set_kshard restricts Solve and the projectors to flat k in [k_begin, k_end);
+ * set_bands installs the all-gathered Bands (numb x Nk) before the sort so every rank finds the
+ * same Fermi level; project_local forms this rank's share of P_new = (window + bulk)/Nk over its
+ * k points (zFock: host copy, NULL allowed), and set_pnew loads the all-reduced P_new for
+ * forge_gpu_optimal_step / forge_gpu_mix_potential. */
+int forge_gpu_set_kshard(forge_ctx* ctx, int64_t k_begin, int64_t k_end);
+int forge_gpu_set_bands(forge_ctx* ctx, const double* Bands);
+int forge_gpu_project_local(forge_ctx* ctx, double* zFock);
+int forge_gpu_set_pnew(forge_ctx* ctx, const double* zFock);
+
 /* SortEnergies_1Spin (HartreeFock.f90:885-925) of the last Solve: SortedEnergies (numb*Nk),
  * nSortedMomenta (numb*Nk x 2), nSortedIndex (numb*Nk, the reference's flattened index
  * icount = (band-1)*Nk + k, 1-based); any output may be NULL. */
