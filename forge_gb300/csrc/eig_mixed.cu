@@ -201,17 +201,26 @@ struct Her2kTcEpi {
     __device__ void operator()(int64_t b, int64_t row, int64_t col0, const float* v, int64_t M, int64_t N) const {
         const int64_t i = row >> 1;
         const bool even = (row & 1) == 0;
-        float2* Ab = A + b * strideA;
+        float im[32];
+#pragma unroll
+        for (int q = 0; q < 32; ++q) im[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
+        if (!even || row >= M) return;
+        float2* __restrict__ base = A + b * strideA + (r0 + i);
+        // all 32 loads first (independent), then the updates: no load waits behind a store
+        float2 old[32];
 #pragma unroll
         for (int q = 0; q < 32; ++q) {
-            const float im = __shfl_xor_sync(0xffffffffu, v[q], 1);
             const int64_t j = col0 + q;
-            if (even && row < M && j < N && j <= i) {
-                float2* x = Ab + (r0 + i) + (r0 + j) * lda;
-                float2 y = *x;
+            old[q] = (j < N && j <= i) ? base[(r0 + j) * lda] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+            const int64_t j = col0 + q;
+            if (j < N && j <= i) {
+                float2 y = old[q];
                 y.x -= v[q];
-                y.y = (i == j) ? 0.f : y.y - im;
-                *x = y;
+                y.y = (i == j) ? 0.f : y.y - im[q];
+                base[(r0 + j) * lda] = y;
             }
         }
     }
@@ -389,22 +398,39 @@ struct BtXEpi {
         const int64_t rr = row >> 1, r = j0 + rr;
         const bool even = (row & 1) == 0;
         const size_t P = (size_t)n4 * iu;
-        float* X = Xs + b * 4 * P;
-#pragma unroll 4
-        for (int q = 0; q < 32; ++q) {
-            const float im = __shfl_xor_sync(0xffffffffu, v[q], 1);
-            const int64_t c = col0 + q;
-            if (even && row < M && r < n && c < iu) {
-                const size_t o = (size_t)c * n4 + r;
-                const float xr = (X[o] + X[2 * P + o]) - v[q];
-                const float xi = (X[P + o] + X[3 * P + o]) - im;
-                float h, l;
-                split2(xr, h, l);
-                X[o] = h;
-                X[2 * P + o] = l;
-                split2(xi, h, l);
-                X[P + o] = h;
-                X[3 * P + o] = l;
+        float* __restrict__ X = Xs + b * 4 * P;
+        float im[32];
+#pragma unroll
+        for (int q = 0; q < 32; ++q) im[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
+        if (!even || row >= M || r >= n) return;
+        // two half-chunks of 16 columns: 64 independent loads, then the re-split stores
+#pragma unroll
+        for (int h0 = 0; h0 < 32; h0 += 16) {
+            float hr[16], hi[16], lr[16], li[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int64_t c = col0 + h0 + q;
+                const size_t o = (size_t)(c < iu ? c : 0) * n4 + r;
+                hr[q] = X[o];
+                hi[q] = X[P + o];
+                lr[q] = X[2 * P + o];
+                li[q] = X[3 * P + o];
+            }
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int64_t c = col0 + h0 + q;
+                if (c < iu) {
+                    const size_t o = (size_t)c * n4 + r;
+                    const float xr = (hr[q] + lr[q]) - v[h0 + q];
+                    const float xi = (hi[q] + li[q]) - im[h0 + q];
+                    float h, l;
+                    split2(xr, h, l);
+                    X[o] = h;
+                    X[2 * P + o] = l;
+                    split2(xi, h, l);
+                    X[P + o] = h;
+                    X[3 * P + o] = l;
+                }
             }
         }
     }

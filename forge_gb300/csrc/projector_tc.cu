@@ -46,45 +46,80 @@ __global__ void k_stage_proj(const double2* __restrict__ X, int64_t ldx, int64_t
     }
 }
 
-struct ProjTcEpi {
-    double2* P;     // 4 x n x n
+// GEMM epilogue: the lower triangle of Re C or Im C, plain coalesced stores (column-major n x n)
+struct ProjStoreEpi {
+    float* C;
     int64_t n;
-    double2 ph[4];
-    int imag;       // 0: v = Re C, 1: v = Im C
     __device__ void operator()(int64_t b, int64_t row, int64_t col0, const float* v, int64_t M, int64_t N) const {
         (void)b;
-        const int64_t i = row;
-        if (i >= M) return;
-        const size_t NN = (size_t)n * n;
-#pragma unroll 4
+        if (row >= M) return;
+#pragma unroll
         for (int q = 0; q < 32; ++q) {
             const int64_t j = col0 + q;
-            if (j >= N || j > i || (imag && j == i)) continue;
-            const double c = (double)v[q];
-            const size_t oij = i + (size_t)j * n, oji = j + (size_t)i * n;
-#pragma unroll
-            for (int cc = 0; cc < 4; ++cc) {
-                const double2 p = ph[cc];
-                double2 a, t;
-                if (!imag) {
-                    a = make_double2(p.x * c, p.y * c);       // ph * Re C
-                    t = a;                                    // (j,i): ph * conj(C) has the same real part
-                } else {
-                    a = make_double2(-p.y * c, p.x * c);      // ph * (i Im C)
-                    t = make_double2(p.y * c, -p.x * c);      // ph * (-i Im C)
-                }
-                double2* x = P + cc * NN + oij;
-                *x = make_double2(x->x + a.x, x->y + a.y);
-                if (i != j) {
-                    double2* y = P + cc * NN + oji;
-                    *y = make_double2(y->x + t.x, y->y + t.y);
-                }
-            }
+            if (j < N && j <= row) C[row + j * n] = v[q];
         }
     }
 };
 
-size_t proj_tc_workspace_floats(int64_t n, int64_t iu) { return 6 * (size_t)n * ((iu + 3) / 4 * 4) + 64; }
+// P_c += ph_c C on tile (bi, bj) and P_c += ph_c conj(C) on the mirrored tile (bj, bi), for the
+// Hermitian C of which only the lower triangle (Cr, Ci) was formed; 32 x 32 tiles, coalesced.
+__global__ void __launch_bounds__(256) k_proj_accum(double2* __restrict__ P, const float* __restrict__ Cr,
+                                                    const float* __restrict__ Ci, int64_t n, double2 ph0,
+                                                    double2 ph1, double2 ph2, double2 ph3) {
+    const int64_t bi = blockIdx.x, bj = blockIdx.y;
+    if (bi < bj) return;
+    __shared__ float sr[32][33], si[32][33];
+    const int64_t i0 = bi * 32, j0 = bj * 32;
+    for (int y = threadIdx.y; y < 32; y += 8) {
+        const int64_t i = i0 + threadIdx.x, j = j0 + y;
+        const bool ok = i < n && j < n && i >= j;
+        sr[y][threadIdx.x] = ok ? Cr[i + j * n] : 0.f;                 // sr[col][row]
+        si[y][threadIdx.x] = (ok && i != j) ? Ci[i + j * n] : 0.f;
+    }
+    __syncthreads();
+    const double2 ph[4] = {ph0, ph1, ph2, ph3};
+    const size_t NN = (size_t)n * n;
+    // tile (bi, bj): element (i, j) = C(i, j) if i >= j else conj(C(j, i)) (diagonal tile only)
+    for (int y = threadIdx.y; y < 32; y += 8) {
+        const int64_t i = i0 + threadIdx.x, j = j0 + y;
+        if (i >= n || j >= n) continue;
+        double cr, ci;
+        if (i >= j) {
+            cr = sr[y][threadIdx.x];
+            ci = si[y][threadIdx.x];
+        } else {
+            cr = sr[threadIdx.x][y];
+            ci = -si[threadIdx.x][y];
+        }
+        const size_t o = i + (size_t)j * n;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            double2 p = P[c * NN + o];
+            p.x += ph[c].x * cr - ph[c].y * ci;
+            p.y += ph[c].x * ci + ph[c].y * cr;
+            P[c * NN + o] = p;
+        }
+    }
+    if (bi == bj) return;
+    // mirrored tile (bj, bi): element (j, i) = conj(C(i, j))
+    for (int y = threadIdx.y; y < 32; y += 8) {
+        const int64_t j = j0 + threadIdx.x, i = i0 + y;
+        if (i >= n || j >= n) continue;
+        const double cr = sr[threadIdx.x][y], ci = -si[threadIdx.x][y];
+        const size_t o = j + (size_t)i * n;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            double2 p = P[c * NN + o];
+            p.x += ph[c].x * cr - ph[c].y * ci;
+            p.y += ph[c].x * ci + ph[c].y * cr;
+            P[c * NN + o] = p;
+        }
+    }
+}
+
+size_t proj_tc_workspace_floats(int64_t n, int64_t iu) {
+    return 6 * (size_t)n * ((iu + 3) / 4 * 4) + 2 * (size_t)n * n + 128;
+}
 
 // P_c += ph_c * conj(X) X^T over the first K columns of X (n x K, ldx) on the tensor cores.
 int bulk_projector_tc(cudaStream_t st, const double2* X, int64_t ldx, int64_t n, int64_t K, int64_t iu,
@@ -109,10 +144,14 @@ int bulk_projector_tc(cudaStream_t st, const double2* X, int64_t ldx, int64_t n,
     const int32_t za[6] = {0, 1, 0, 1, 2, 3};     // A: hi.re hi.im hi.re hi.im lo.re lo.im
     const int32_t zbr[6] = {0, 1, 2, 3, 0, 1};    // B for Re C: hi.re hi.im lo.re lo.im hi.re hi.im
     const int32_t zbi[6] = {1, 4, 3, 5, 1, 4};    // B for Im C: hi.im -hi.re lo.im -lo.re hi.im -hi.re
-    ProjTcEpi er{P, n, {ph[0], ph[1], ph[2], ph[3]}, 0};
-    ProjTcEpi ei{P, n, {ph[0], ph[1], ph[2], ph[3]}, 1};
-    FORGE_TRY(tc_gemm_tf32_mapped(st, op, mk(za), op, mk(zbr), 1, 1, er, err));
-    FORGE_TRY(tc_gemm_tf32_mapped(st, op, mk(za), op, mk(zbi), 1, 1, ei, err));
+    float* Cr = ws + 6 * (size_t)n * ldk;
+    Cr = (float*)(((uintptr_t)Cr + 255) & ~(uintptr_t)255);
+    float* Ci = Cr + (size_t)n * n;
+    FORGE_TRY(tc_gemm_tf32_mapped(st, op, mk(za), op, mk(zbr), 1, 1, ProjStoreEpi{Cr, n}, err));
+    FORGE_TRY(tc_gemm_tf32_mapped(st, op, mk(za), op, mk(zbi), 1, 1, ProjStoreEpi{Ci, n}, err));
+    const unsigned nt = (unsigned)((n + 31) / 32);
+    k_proj_accum<<<dim3(nt, nt), dim3(32, 8), 0, st>>>(P, Cr, Ci, n, ph[0], ph[1], ph[2], ph[3]);
+    FORGE_LAUNCH_CHECK();
     const double nd = (double)n;
     prof_end(ST_PROJECTOR, nd * K * 16.0 + 2.0 * 4.0 * 2.0 * nd * nd * 16.0, 2.0 * 2.0 * nd * nd * 6.0 * K / 2.0);
     return 0;

@@ -3,7 +3,7 @@
 //   D[b](m, n) = sum_k A[b](m, k) * B[b](n, k)        (both operands K-major, fp32 storage read as tf32)
 //
 // One CTA (128 threads) per 128 x 128 output tile:
-//   warp 0 / lane 0 : TMA producer (cp.async.bulk.tensor.3d, 128B swizzle, 4-stage ring)
+//   warp 0 / lane 0 : TMA producer (cp.async.bulk.tensor.3d, 128B swizzle, 3-stage ring)
 //   warp 1 / lane 0 : MMA issuer   (tcgen05.mma.cta_group::1.kind::tf32, M=128 N=128 K=8)
 //   all 4 warps     : epilogue     (tcgen05.ld.32x32b.x32 -> registers -> functor)
 // TMEM: 128 columns allocated by warp 0.  Every mbarrier wait is bounded; on timeout the
@@ -21,7 +21,9 @@
 
 namespace forge {
 
-constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 32, TC_STAGES = 4, TC_THREADS = 128;
+// 3 stages x 32 KB + barriers keeps two CTAs resident per SM (2 x 128 TMEM columns), so one
+// tile's epilogue overlaps the other's main loop.
+constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 32, TC_STAGES = 3, TC_THREADS = 128;
 constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 4;  // 16 KB per operand per stage
 constexpr int TC_SMEM = TC_STAGES * 2 * TC_TILE_BYTES + 1024 + 256;
 constexpr uint32_t TC_SPIN_LIMIT = 1u << 26;     // bounded waits (>> any legitimate wait)
@@ -122,7 +124,7 @@ __device__ inline void tc_commit(uint64_t* bar) {
 }
 
 template <class EPI>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+__global__ void __launch_bounds__(TC_THREADS, 2)
     k_tc_gemm_tf32(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int64_t M,
                    int64_t N, TcKMap ka, TcKMap kb_map, int64_t lower_div, EPI epi, int* err) {
     // lower_div > 0: skip tiles whose rows (divided by lower_div) all lie above the diagonal

@@ -140,66 +140,75 @@ __global__ void __launch_bounds__(256) k_trd_hemv(TrdArgs<T> a, int64_t p, int i
     const int64_t c0 = col + 1;
     const int64_t t = blockIdx.x;
     if (t < ntiles) {
-        // tile (bi, bj), bi >= bj, of the trailing matrix A(c0:n, c0:n)
-        int64_t bi = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-        while ((bi + 1) * (bi + 2) / 2 <= t) ++bi;
-        while (bi * (bi + 1) / 2 > t) --bi;
-        const int64_t bj = t - bi * (bi + 1) / 2;
-        const int64_t R0 = c0 + bi * TRD_TILE, C0 = c0 + bj * TRD_TILE;
-        __shared__ V vr[TRD_TILE], vc[TRD_TILE];
-        __shared__ V rsum[4][TRD_TILE];
-        __shared__ V csum[2][TRD_TILE];
-        if (threadIdx.x < TRD_TILE) {
-            int64_t r = R0 + threadIdx.x;
+        // tile (bi, bj) of the trailing matrix A(c0:n, c0:n): rows [128 bi, 128 bi + 128), columns
+        // [64 bj, 64 bj + 64); row block bi holds the column blocks bj <= 2 bi + 1 (prefix bi (bi+1))
+        int64_t bi = (int64_t)((sqrt(4.0 * (double)t + 1.0) - 1.0) * 0.5);
+        while ((bi + 1) * (bi + 2) <= t) ++bi;
+        while (bi * (bi + 1) > t) --bi;
+        const int64_t bj = t - bi * (bi + 1);
+        const int64_t R0 = c0 + bi * HV_RB, C0 = c0 + bj * HV_CB;
+        __shared__ V vr[HV_RB], vc[HV_CB];
+        __shared__ V rsum[4][HV_RB];
+        __shared__ V cs[64][HV_CB + 1];
+        __shared__ V cq[4][HV_CB];
+        if (threadIdx.x < HV_RB) {
+            const int64_t r = R0 + threadIdx.x;
             vr[threadIdx.x] = (r < n) ? trd_v<T>(A, lda, col, r, sr, si) : vzero<V>();
-        } else if (threadIdx.x < 2 * TRD_TILE) {
-            int64_t c = C0 + threadIdx.x - TRD_TILE;
-            vc[threadIdx.x - TRD_TILE] = (c < n) ? trd_v<T>(A, lda, col, c, sr, si) : vzero<V>();
+        } else if (threadIdx.x < HV_RB + HV_CB) {
+            const int64_t c = C0 + threadIdx.x - HV_RB;
+            vc[threadIdx.x - HV_RB] = (c < n) ? trd_v<T>(A, lda, col, c, sr, si) : vzero<V>();
+        }
+        const int tr = threadIdx.x & 63, tg = threadIdx.x >> 6;
+        const int64_t r0 = R0 + tr, r1 = R0 + 64 + tr;
+        // 32 loads per thread (rows r0 and r1, 16 columns) issued before any arithmetic
+        V a0[16], a1[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int64_t c = C0 + tg * 16 + q;
+            a0[q] = (r0 < n && c < n && c <= r0) ? A[r0 + c * lda] : vzero<V>();
+            a1[q] = (r1 < n && c < n && c <= r1) ? A[r1 + c * lda] : vzero<V>();
         }
         __syncthreads();
-        const int tr = threadIdx.x & 63, tg = threadIdx.x >> 6;
-        const int64_t row = R0 + tr;
-        const bool diag = (bi == bj);
-        // all 16 loads of this thread are issued before any arithmetic
-        V av[16];
+        V racc0 = vzero<V>(), racc1 = vzero<V>();
+        const V v0 = vr[tr], v1 = vr[64 + tr];
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
             const int64_t c = C0 + tg * 16 + q;
-            av[q] = (row < n && c < n && (!diag || c <= row)) ? A[row + c * lda] : vzero<V>();
+            V x0 = a0[q], x1 = a1[q];
+            const bool d0 = (c == r0), d1 = (c == r1);
+            if (d0) x0.y = 0;
+            if (d1) x1.y = 0;
+            const V vcq = vc[tg * 16 + q];
+            racc0 = vadd(racc0, vmul(x0, vcq));
+            racc1 = vadd(racc1, vmul(x1, vcq));
+            // column part: conj(A(r, c)) v_r for r > c (the diagonal belongs to the row part only)
+            V s = d0 ? vzero<V>() : vcjmul(x0, v0);
+            if (!d1) s = vadd(s, vcjmul(x1, v1));
+            cs[tr][tg * 16 + q] = s;
         }
-        V racc = vzero<V>();
-        V cacc[16];
-        const V vrow = vr[tr];
+        rsum[tg][tr] = racc0;
+        rsum[tg][64 + tr] = racc1;
+        __syncthreads();
+        {
+            // column sums: thread (col, quarter of the 64 row pairs)
+            const int c = threadIdx.x & 63, qt = threadIdx.x >> 6;
+            V s = vzero<V>();
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            const int64_t c = C0 + tg * 16 + q;
-            V x = av[q];
-            const bool on_diag = diag && (c == row);
-            if (on_diag) x.y = 0;
-            racc = vadd(racc, vmul(x, vc[tg * 16 + q]));
-            cacc[q] = on_diag ? vzero<V>() : vcjmul(x, vrow);
-        }
-        rsum[tg][tr] = racc;
-        const int lane = threadIdx.x & 31, half = (threadIdx.x >> 5) & 1;
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            V s = warp_sum(cacc[q]);
-            if (lane == 0) csum[half][tg * 16 + q] = s;
+            for (int i = 0; i < 16; ++i) s = vadd(s, cs[qt * 16 + i][c]);
+            cq[qt][c] = s;
         }
         __syncthreads();
         V* Yrow = a.Yrow + b * a.ystride;
         V* Ycol = a.Ycol + b * a.ystride;
-        if (threadIdx.x < TRD_TILE) {
-            int64_t r = R0 + threadIdx.x;
-            if (r < n) {
-                V s = vadd(vadd(rsum[0][threadIdx.x], rsum[1][threadIdx.x]),
-                           vadd(rsum[2][threadIdx.x], rsum[3][threadIdx.x]));
-                Yrow[bj * n + r] = s;
-            }
-        } else if (threadIdx.x < 2 * TRD_TILE) {
-            int q = threadIdx.x - TRD_TILE;
-            int64_t c = C0 + q;
-            if (c < n) Ycol[bi * n + c] = vadd(csum[0][q], csum[1][q]);
+        if (threadIdx.x < HV_RB) {
+            const int64_t r = R0 + threadIdx.x;
+            if (r < n)
+                Yrow[bj * n + r] = vadd(vadd(rsum[0][threadIdx.x], rsum[1][threadIdx.x]),
+                                        vadd(rsum[2][threadIdx.x], rsum[3][threadIdx.x]));
+        } else if (threadIdx.x < HV_RB + HV_CB) {
+            const int q = threadIdx.x - HV_RB;
+            const int64_t c = C0 + q;
+            if (c < n) Ycol[bi * n + c] = vadd(vadd(cq[0][q], cq[1][q]), vadd(cq[2][q], cq[3][q]));
         }
     } else {
         // panel dots over rows [c0 + rb*256, ...): s1 = W^H v, s2 = V^H v
@@ -265,12 +274,13 @@ __global__ void __launch_bounds__(TRD_ROWS) k_trd_finish(TrdArgs<T> a, int64_t p
     const int rr = threadIdx.x & 31, sl = threadIdx.x >> 5;
     const int64_t r = c0 + (int64_t)blockIdx.x * 32 + rr;
     if (r < n) {
-        const int64_t B = (r - c0) / TRD_TILE;
+        // row part from the tiles (blk128(r), bj <= blk64(r)); column part from (bi >= blk128(r), blk64(r))
+        const int64_t Bc = (r - c0) / HV_CB, Br = (r - c0) / HV_RB;
         const V* Yrow = a.Yrow + b * a.ystride;
         const V* Ycol = a.Ycol + b * a.ystride;
         V y = vzero<V>();
-        for (int64_t q = sl; q <= B; q += 8) y = vadd(y, Yrow[q * n + r]);
-        for (int64_t q = B + sl; q < nb2; q += 8) y = vadd(y, Ycol[q * n + r]);
+        for (int64_t q = sl; q <= Bc; q += 8) y = vadd(y, Yrow[q * n + r]);
+        for (int64_t q = Br + sl; q < nb2; q += 8) y = vadd(y, Ycol[q * n + r]);
         ysl[sl][rr] = y;
     }
     __syncthreads();
@@ -391,8 +401,9 @@ int tridiagonalize(cudaStream_t st, TrdArgs<T>& a, int64_t batch) {
             if (!has_refl) continue;
             ++nrefl;
             const int64_t n2 = n - col - 1;
-            const int64_t nb2 = (n2 + TRD_TILE - 1) / TRD_TILE;
-            const int64_t ntiles = nb2 * (nb2 + 1) / 2;
+            const int64_t nbr = (n2 + HV_RB - 1) / HV_RB;   // 128-row blocks
+            const int64_t nbc = (n2 + HV_CB - 1) / HV_CB;   // 64-column blocks (nbc <= 2 nbr)
+            const int64_t ntiles = (nbr - 1) * nbr + nbc;   // row block bi holds min(2 bi + 2, nbc) tiles
             const int64_t nrb = (n2 + 255) / 256;
             dim3 gb((unsigned)(ntiles + (ii > 0 ? nrb : 0)), (unsigned)batch);
             prof_begin(ST_HEMV);
@@ -403,7 +414,7 @@ int tridiagonalize(cudaStream_t st, TrdArgs<T>& a, int64_t batch) {
             dim3 gf((unsigned)((n2 + 31) / 32), (unsigned)batch);
             dim3 gc((unsigned)((n2 + TRD_ROWS - 1) / TRD_ROWS), (unsigned)batch);
             prof_begin(ST_TRD_FINISH);
-            k_trd_finish<T><<<gf, TRD_ROWS, 0, st>>>(a, p, ii, col, nb2, ii > 0 ? nrb : 0);
+            k_trd_finish<T><<<gf, TRD_ROWS, 0, st>>>(a, p, ii, col, nbr, ii > 0 ? nrb : 0);
             FORGE_LAUNCH_CHECK();
             k_trd_fix<T><<<gc, TRD_ROWS, 0, st>>>(a, ii, col);
             FORGE_LAUNCH_CHECK();
