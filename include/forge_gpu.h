@@ -230,6 +230,21 @@ int forge_gpu_mlp_gradient(forge_mlp* mlp, const float* X, const float* targets,
 int forge_gpu_mlp_train(forge_mlp* mlp, const float* X, const float* targets, int64_t n, int64_t epochs,
                         int64_t batch, double lr, uint64_t seed, float* last_loss);
 
+/* Allocation-free eigen-solver (no counterpart in the reference): zdiagRed for one Hermitian
+ * matrix (lower triangle of A, n x n complex, column-major) for callers that cannot allocate
+ * device memory at call time (a memory pool or arena owning the whole GPU, latency-critical
+ * loops where cudaMalloc would synchronise, hosts that manage every device buffer themselves).
+ * A (overwritten), w (iu eigenvalues) and Z (n x iu complex eigenvectors) are DEVICE pointers;
+ * stream is a cudaStream_t (NULL = default stream).  The workspace is a static device array of
+ * FORGE_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library, so n is limited to
+ * FORGE_NOALLOC_MAX_N; larger n is rejected with FORGE_ERR_ARG.  The first call on a device looks
+ * up the array's device address: make it before any stream capture.  Calls share the array:
+ * calls whose work overlaps on the GPU race.  Returns 0, 1 (inverse iteration did not converge)
+ * or FORGE_ERR_*.  The solver is the FP64 path of forge_gpu_zheevr_batch. */
+#define FORGE_NOALLOC_MAX_N 512
+#define FORGE_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+int forge_gpu_zheevr_noalloc(double* A, int64_t n, int64_t iu, double* w, double* Z, void* stream);
+
 /* Synchronises the context's stream (for host timing). */
 int forge_gpu_synchronize(forge_ctx* ctx);
 
