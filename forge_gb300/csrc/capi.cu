@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -108,10 +109,21 @@ int choose_batch(forge_ctx* x) {
     if (c.precision == FORGE_PREC_MIXED) per_k += eig_mixed_workspace_bytes(N, iu, 1);
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
-    size_t budget = freeb > (size_t)8 << 30 ? (freeb - ((size_t)8 << 30)) / 2 : freeb / 4;
+    // kept free: 8 GB headroom, the eigenvectors of every k, the four bulk cells and the
+    // projector / window work arrays allocated after the batch is chosen
+    const size_t reserve = ((size_t)8 << 30) + (size_t)c.Nk * N * iu * 16 + (size_t)10 * N * N * 16;
+    const size_t budget = freeb > reserve ? freeb - reserve : freeb / 4;
     int64_t b = (int64_t)(budget / per_k);
+    // FORGE_EIG_BATCH caps the number of k points solved per launch (memory control)
+    if (const char* env = std::getenv("FORGE_EIG_BATCH")) {
+        const long cap = std::strtol(env, nullptr, 10);
+        if (cap > 0 && cap < b) b = cap;
+    }
     if (b < 1) b = 1;
     if (b > c.Nk) b = c.Nk;
+    // equal batches: ceil(Nk / b) launches of (nearly) the same size
+    const int64_t nbatches = (c.Nk + b - 1) / b;
+    b = (c.Nk + nbatches - 1) / nbatches;
     return (int)b;
 }
 

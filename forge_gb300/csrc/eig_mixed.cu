@@ -11,6 +11,8 @@
 //     X -= V (T W) on the tensor cores with the same split; X lives in four TF32 planes
 //     (hi.re, hi.im, lo.re, lo.im) that the second GEMM's epilogue re-splits in place.
 //  5. X -> complex128 for the projectors.
+#include <algorithm>
+
 #include "cvec.cuh"
 #include "eig.cuh"
 #include "tc_gemm.cuh"
@@ -19,6 +21,18 @@
 namespace forge {
 
 constexpr int BT_NB = 64;   // reflectors per back-transform block
+constexpr int64_t BT_CTA_TARGET = 2 * 152;  // CTAs that fill the GPU (two resident per SM)
+
+// Upper bounds of the K splits of the two long-K back-transform products (they size the
+// workspace): the Gram matrix V^H V (one 64 x 64 tile per matrix, no split shorter than 256
+// rows) and W = V^H X on the tensor cores (iu/128 tiles per matrix, >= 8 K blocks per split).
+inline void bt_split_caps(int64_t n, int64_t iu, int64_t batch, int64_t& ksg, int64_t& ksw) {
+    ksg = std::min<int64_t>(std::min<int64_t>(32, (BT_CTA_TARGET + batch - 1) / batch), (n + 255) / 256);
+    const int64_t tiles = (iu + TC_BN - 1) / TC_BN * batch;
+    ksw = std::min<int64_t>(std::min<int64_t>(16, (BT_CTA_TARGET + tiles - 1) / tiles),
+                            std::max<int64_t>(1, 6 * ((n + 31) / 32) / 8));
+    ksg = std::max<int64_t>(1, ksg);
+}
 constexpr int HK = 384;     // K'' of the split rank-2k update: 3 splits x (re, im) x 2 x TRD_NB
 
 __device__ inline float tf32_hi(float x) {
@@ -79,9 +93,11 @@ void carve(MixedWs& w, Carve& c) {
     w.A1 = c.take<float>(B * 2 * BT_NB * 6 * w.Kp);
     w.A2 = c.take<float>(B * 2 * n * 6 * BT_NB);
     w.B2 = c.take<float>(B * iu * 6 * BT_NB);
-    w.Wb = c.take<float2>(B * BT_NB * iu);
+    int64_t ksg, ksw;
+    bt_split_caps(n, iu, B, ksg, ksw);
+    w.Wb = c.take<float2>(ksw * B * BT_NB * iu);
     w.W2 = c.take<float2>(B * BT_NB * iu);
-    w.G = c.take<float2>(B * BT_NB * BT_NB);
+    w.G = c.take<float2>(ksg * B * BT_NB * BT_NB);
     w.T = c.take<float2>(B * BT_NB * BT_NB);
     w.err = c.take<int>(1);
 }
@@ -272,6 +288,14 @@ struct StoreF2 {
     int64_t ld, stride;
     __device__ void operator()(int64_t i, int64_t j, float2 c) const { G[blockIdx.z * stride + i + j * ld] = c; }
 };
+// partial Gram of K split s of batch item b at G + (s * batch + b) * BT_NB^2
+struct StoreGramSplit {
+    float2* G;
+    int64_t batch;
+    __device__ void operator()(int64_t s, int64_t i, int64_t j, float2 c) const {
+        G[(s * batch + blockIdx.z) * BT_NB * BT_NB + i + j * BT_NB] = c;
+    }
+};
 struct TWa {
     const float2* T;
     int64_t nbk;
@@ -280,27 +304,40 @@ struct TWa {
         return T[blockIdx.z * BT_NB * BT_NB + l + q * BT_NB];
     }
 };
+// W(q, c) as the sum of the ks K-split partials of V^H X (partial z = b * ks + s)
 struct TWb {
     const float2* W;
-    int64_t nbk, iu;
+    int64_t nbk, iu, ks;
     __device__ float2 operator()(int64_t c, int64_t q) const {
         if (q >= nbk || c >= iu) return make_float2(0.f, 0.f);
-        return W[blockIdx.z * BT_NB * iu + q + c * BT_NB];
+        const float2* p = W + (blockIdx.z * ks) * BT_NB * iu + q + c * BT_NB;
+        float2 acc = p[0];
+        for (int64_t s = 1; s < ks; ++s) acc = vadd(acc, p[s * BT_NB * iu]);
+        return acc;
     }
 };
 
-__global__ void k_larft32(const float2* __restrict__ G, const float2* __restrict__ tau, int64_t n, int64_t j0,
-                          int64_t nbk, float2* __restrict__ T) {
+// T of the compact-WY form from the Gram matrix G = V^H V, given as ks K-split partials
+// (partial s of batch item b at G + (s * batch + b) * BT_NB^2).  blockDim.x = BT_NB.
+__global__ void k_larft32(const float2* __restrict__ G, int64_t ks, int64_t batch, const float2* __restrict__ tau,
+                          int64_t n, int64_t j0, int64_t nbk, float2* __restrict__ T) {
     const int64_t b = blockIdx.x;
-    const float2* Gb = G + b * BT_NB * BT_NB;
     float2* Tb = T + b * BT_NB * BT_NB;
     const float2* tb = tau + b * n;
     __shared__ float2 tmp[BT_NB];
-    for (int q = threadIdx.x; q < BT_NB * BT_NB; q += blockDim.x) Tb[q] = make_float2(0.f, 0.f);
+    __shared__ float2 Gs[BT_NB][BT_NB + 1];   // Gs[i][r] = G(r, i), upper part r < i
+    for (int q = threadIdx.x; q < BT_NB * BT_NB; q += blockDim.x) {
+        Tb[q] = make_float2(0.f, 0.f);
+        const int r = q % BT_NB, i = q / BT_NB;
+        float2 acc = make_float2(0.f, 0.f);
+        if (r < i)
+            for (int64_t s = 0; s < ks; ++s) acc = vadd(acc, G[(s * batch + b) * BT_NB * BT_NB + q]);
+        Gs[i][r] = acc;
+    }
     __syncthreads();
     for (int64_t i = 0; i < nbk; ++i) {
         const float2 ti = tb[j0 + i];
-        if (threadIdx.x < i) tmp[threadIdx.x] = vmul(make_float2(-ti.x, -ti.y), Gb[threadIdx.x + i * BT_NB]);
+        if (threadIdx.x < i) tmp[threadIdx.x] = vmul(make_float2(-ti.x, -ti.y), Gs[i][threadIdx.x]);
         __syncthreads();
         if (threadIdx.x < i) {
             float2 s = make_float2(0.f, 0.f);
@@ -334,11 +371,12 @@ __global__ void k_stage_bt1(const float2* __restrict__ A, int64_t lda, int64_t s
     im[4 * Kp + kk] = -vil; im[5 * Kp + kk] = vrl;
 }
 
-// GEMM1 epilogue: W(l, c) = (row 2l, row 2l+1)
+// GEMM1 epilogue: W(l, c) = (row 2l, row 2l+1) of K-split partial z = b * ks + s
 struct BtW1Epi {
     float2* W;
     int64_t nbk, iu;
-    __device__ void operator()(int64_t b, int64_t row, int64_t col0, const float* v, int64_t M, int64_t N) const {
+    __device__ void operator()(int64_t z, int64_t row, int64_t col0, const float* v, int64_t M, int64_t N) const {
+        const int64_t b = z;   // partial index
         const int64_t l = row >> 1;
         const bool even = (row & 1) == 0;
 #pragma unroll
@@ -441,17 +479,22 @@ int backtransform_tc(cudaStream_t st, MixedWs& ws, int64_t batch) {
     const int64_t nrefl = n - 1;
     const int64_t nblocks = (nrefl + BT_NB - 1) / BT_NB;
     const int64_t lda = n, strideA = n * n;
+    int64_t ksg_cap, ksw_cap;
+    bt_split_caps(n, iu, batch, ksg_cap, ksw_cap);
     for (int64_t blk = nblocks - 1; blk >= 0; --blk) {
         const int64_t j0 = blk * BT_NB;
         const int64_t nbk = (nrefl - j0 < BT_NB) ? (nrefl - j0) : BT_NB;
         const int64_t Krows = n - j0;                      // rows j0 .. n-1
         const int64_t nkp = (Krows + 31) / 32;
         const int64_t Kp = nkp * 32;
-        // Gram and compact-WY factor (CUDA cores, FP32)
-        FORGE_TRY((zgemm_launch<float2, KMAJOR, KMAJOR, false>(
-            st, BT_NB, BT_NB, Krows, batch, BtGA{ws.A32, lda, strideA, n, j0, nbk},
-            BtGB{ws.A32, lda, strideA, n, j0, nbk}, StoreF2{ws.G, BT_NB, BT_NB * BT_NB})));
-        k_larft32<<<(unsigned)batch, 64, 0, st>>>(ws.G, ws.tau, n, j0, nbk, ws.T);
+        int64_t ksw = 1;
+        // Gram (CUDA cores, FP32, split over K to fill the GPU) and compact-WY factor
+        const int64_t kg_want = std::min<int64_t>(ksg_cap, (Krows + 255) / 256);
+        const int64_t ksg = zg_ksplit_count(Krows, kg_want);
+        FORGE_TRY((zgemm_launch_splitk<float2, KMAJOR, KMAJOR>(
+            st, BT_NB, BT_NB, Krows, batch, kg_want, BtGA{ws.A32, lda, strideA, n, j0, nbk},
+            BtGB{ws.A32, lda, strideA, n, j0, nbk}, StoreGramSplit{ws.G, batch})));
+        k_larft32<<<(unsigned)batch, BT_NB, 0, st>>>(ws.G, ksg, batch, ws.tau, n, j0, nbk, ws.T);
         FORGE_LAUNCH_CHECK();
         // W = V^H X  (tensor cores)
         k_stage_bt1<<<dim3((unsigned)((Kp + 255) / 256), BT_NB, (unsigned)batch), 256, 0, st>>>(
@@ -468,11 +511,14 @@ int backtransform_tc(cudaStream_t st, MixedWs& ws, int64_t batch) {
             kb.zbatch = 4;
             const int32_t zs[6] = {0, 1, 2, 3, 0, 1};
             for (int q = 0; q < 6; ++q) kb.zsel[q] = zs[q];
-            FORGE_TRY(tc_gemm_tf32_mapped(st, A, ka, B, kb, batch, 0, BtW1Epi{ws.Wb, nbk, iu}, ws.err));
+            // split K so that the (1 x iu/128 x batch) tile grid fills the GPU
+            const int want = (int)std::min<int64_t>(ksw_cap, std::max<int64_t>(1, 6 * nkp / 8));
+            ksw = tc_ksplit_count(6 * nkp, want);
+            FORGE_TRY(tc_gemm_tf32_mapped(st, A, ka, B, kb, batch, 0, BtW1Epi{ws.Wb, nbk, iu}, ws.err, want));
         }
-        // W2 = T W (CUDA cores)
+        // W2 = T W (CUDA cores; W summed over its K-split partials on load)
         FORGE_TRY((zgemm_launch<float2, IMAJOR, KMAJOR, false>(st, BT_NB, iu, BT_NB, batch, TWa{ws.T, nbk},
-                                                                TWb{ws.Wb, nbk, iu},
+                                                                TWb{ws.Wb, nbk, iu, ksw},
                                                                 StoreF2{ws.W2, BT_NB, BT_NB * iu})));
         // X(j0:, :) -= V W2  (tensor cores)
         k_stage_bt2<<<dim3((unsigned)((Krows * BT_NB + 255) / 256), (unsigned)batch), 256, 0, st>>>(

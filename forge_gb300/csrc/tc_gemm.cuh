@@ -126,7 +126,8 @@ __device__ inline void tc_commit(uint64_t* bar) {
 template <class EPI>
 __global__ void __launch_bounds__(TC_THREADS, 2)
     k_tc_gemm_tf32(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int64_t M,
-                   int64_t N, TcKMap ka, TcKMap kb_map, int64_t lower_div, EPI epi, int* err) {
+                   int64_t N, TcKMap ka, TcKMap kb_map, int64_t lower_div, int32_t ksplit, int32_t kchunk, EPI epi,
+                   int* err) {
     // lower_div > 0: skip tiles whose rows (divided by lower_div) all lie above the diagonal
     if (lower_div > 0 && ((int64_t)blockIdx.x * TC_BM + TC_BM - 1) / lower_div < (int64_t)blockIdx.y * TC_BN) return;
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
@@ -143,8 +144,12 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     volatile int* n_consumed = abort_flag + 2;  // k blocks consumed by the MMA issuer
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t m0 = (int64_t)blockIdx.x * TC_BM, n0 = (int64_t)blockIdx.y * TC_BN, b = blockIdx.z;
-    const int nk = ka.nkp * ka.nseg;
+    // split-K: blockIdx.z = b * ksplit + s; split s runs K blocks [s kchunk, min(nk, (s+1) kchunk))
+    const int64_t m0 = (int64_t)blockIdx.x * TC_BM, n0 = (int64_t)blockIdx.y * TC_BN;
+    const int64_t b = blockIdx.z / ksplit;
+    const int kb_lo = (int)(blockIdx.z - b * ksplit) * kchunk;
+    const int nk_all = ka.nkp * ka.nseg;
+    const int nk = (nk_all - kb_lo < kchunk) ? (nk_all - kb_lo) : kchunk;   // K blocks of this CTA
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TC_STAGES; ++s) {
@@ -179,8 +184,9 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
             if (*abort_flag) break;
             mbar_expect_tx(&full[s], 2 * TC_TILE_BYTES);
             {
-                const int sa = kb / ka.nkp, ra = kb - sa * ka.nkp;
-                const int sb = kb / kb_map.nkp, rb = kb - sb * kb_map.nkp;
+                const int kg = kb_lo + kb;
+                const int sa = kg / ka.nkp, ra = kg - sa * ka.nkp;
+                const int sb = kg / kb_map.nkp, rb = kg - sb * kb_map.nkp;
                 tma_load_3d(sA + s * (TC_TILE_BYTES / 4), &mapA, &full[s], ka.koff + ra * TC_BK, (int32_t)m0,
                             ka.zsel[sa] + ka.zbatch * (int32_t)b);
                 tma_load_3d(sB + s * (TC_TILE_BYTES / 4), &mapB, &full[s], kb_map.koff + rb * TC_BK, (int32_t)n0,
@@ -242,7 +248,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
             float v[32];
 #pragma unroll
             for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
-            epi(b, row, n0 + c0, v, M, N);
+            epi((int64_t)blockIdx.z, row, n0 + c0, v, M, N);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -253,12 +259,22 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     }
 }
 
-// Host launcher: D tiles for b < batch; the epilogue gets (b, row, col0, v[32], M, N) and must
-// bounds-check row < M and col0 + q < N itself.  Both K maps must cover the same number of
-// K blocks.  Every TMA x coordinate (koff + 32 j) is a multiple of 4 floats (16 bytes).
+// Number of K splits actually launched for nk K blocks when `want` are asked for: every split
+// gets ceil(nk / want) blocks, the last one the rest, and none is empty.
+inline int tc_ksplit_count(int64_t nk, int want) {
+    if (want <= 1 || nk <= 1) return 1;
+    const int64_t chunk = (nk + want - 1) / want;
+    return (int)((nk + chunk - 1) / chunk);
+}
+
+// Host launcher: D tiles for b < batch; the epilogue gets (z, row, col0, v[32], M, N) and must
+// bounds-check row < M and col0 + q < N itself; z = b * ks + s, where ks = tc_ksplit_count(nk,
+// ksplit) splits of the K range each produce a partial product (ks = 1 without split-K: z = b).
+// Both K maps must cover the same number of K blocks.  Every TMA x coordinate (koff + 32 j) is
+// a multiple of 4 floats (16 bytes).
 template <class EPI>
 int tc_gemm_tf32_mapped(cudaStream_t st, const TcOperand& A, const TcKMap& ka, const TcOperand& B, const TcKMap& kb,
-                        int64_t batch, int64_t lower_div, const EPI& epi, int* err) {
+                        int64_t batch, int64_t lower_div, const EPI& epi, int* err, int ksplit = 1) {
     if (A.rows <= 0 || B.rows <= 0 || batch <= 0) return 0;
     if ((A.ld % 4) || (B.ld % 4) || (A.batch_stride % 4) || (B.batch_stride % 4) || (ka.koff % 4) || (kb.koff % 4) ||
         ((uintptr_t)A.ptr % 16) || ((uintptr_t)B.ptr % 16)) {
@@ -277,8 +293,17 @@ int tc_gemm_tf32_mapped(cudaStream_t st, const TcOperand& A, const TcKMap& ka, c
         FORGE_CUDA(cudaFuncSetAttribute(k_tc_gemm_tf32<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
         attr_set = true;
     }
-    dim3 grd((unsigned)((A.rows + TC_BM - 1) / TC_BM), (unsigned)((B.rows + TC_BN - 1) / TC_BN), (unsigned)batch);
-    k_tc_gemm_tf32<EPI><<<grd, TC_THREADS, TC_SMEM, st>>>(ma, mb, A.rows, B.rows, ka, kb, lower_div, epi, err);
+    const int64_t nk = (int64_t)ka.nkp * ka.nseg;
+    const int ks = tc_ksplit_count(nk, ksplit);
+    const int32_t kchunk = (int32_t)((nk + ks - 1) / ks);
+    if (batch * ks > 65535) {
+        set_error(FORGE_ERR_ARG, "tc_gemm: batch x K splits exceeds the grid's z extent");
+        return FORGE_ERR_ARG;
+    }
+    dim3 grd((unsigned)((A.rows + TC_BM - 1) / TC_BM), (unsigned)((B.rows + TC_BN - 1) / TC_BN),
+             (unsigned)(batch * ks));
+    k_tc_gemm_tf32<EPI><<<grd, TC_THREADS, TC_SMEM, st>>>(ma, mb, A.rows, B.rows, ka, kb, lower_div, ks, kchunk,
+                                                          epi, err);
     FORGE_LAUNCH_CHECK();
     return 0;
 }

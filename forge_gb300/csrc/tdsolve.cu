@@ -15,6 +15,7 @@
 // ortol is tighter than zstein's 1e-3*||T||_1 (which groups a whole dense spectrum
 // into one serial cluster); with ortol = 1e-7*||T||_1 the vector error bound
 // eps*||T||/gap stays below 1e-8 outside clusters.
+#include <algorithm>
 #include "cvec.cuh"
 #include "eig.cuh"
 #include "zgemm_engine.cuh"
@@ -340,6 +341,20 @@ __global__ void k_z_to_x(const double* __restrict__ Z, int64_t n, int64_t iu, do
 }
 
 // ---------------------------------------------------------------- back-transformation (FP64)
+// Compact-WY blocks of BT64 reflectors; the two long-K products (the Gram matrix V^H V and
+// W = V^H X) are split over K so that their few output tiles still fill the GPU.
+constexpr int BT64 = 64;
+constexpr int64_t BT64_CTA_TARGET = 2 * 152;
+
+// upper bounds of the K splits (they size the workspace): enough CTAs for the GPU, no split
+// shorter than 256 rows
+inline void bt64_split_caps(int64_t n, int64_t iu, int64_t batch, int64_t& ksg, int64_t& ksw) {
+    const int64_t kmax = std::max<int64_t>(1, (n + 255) / 256);
+    ksg = std::min<int64_t>(std::min<int64_t>(32, (BT64_CTA_TARGET + batch - 1) / batch), kmax);
+    const int64_t wt = (iu + ZG_BN - 1) / ZG_BN * batch;
+    ksw = std::min<int64_t>(std::min<int64_t>(16, (BT64_CTA_TARGET + wt - 1) / wt), kmax);
+}
+
 struct BtV {  // V(r, l) of block j0: reflector j0+l, rows >= j0+1 (r relative to j0+1)
     const double2* A;
     int64_t lda, strideA, n, j0, nbk;
@@ -372,20 +387,38 @@ struct BtXk {  // b(c, k) = X(j0+1+k, c)
         return X[blockIdx.z * strideX + r + c * ldx];
     }
 };
-struct BtTW_A {  // a(l, q) = T(l, q) upper triangular, nb x nb column-major
+struct BtTW_A {  // a(l, q) = T(l, q) upper triangular, BT64 x BT64 column-major
     const double2* T;
     int64_t nbk, stride;
     __device__ double2 operator()(int64_t l, int64_t q) const {
         if (l >= nbk || q >= nbk || q < l) return make_double2(0.0, 0.0);
-        return T[blockIdx.z * stride + l + q * TRD_NB];
+        return T[blockIdx.z * stride + l + q * BT64];
     }
 };
-struct BtTW_B {  // b(c, q) = W(q, c)
+struct BtTW_B {  // b(c, q) = W(q, c), W column-major with leading dimension BT64
     const double2* W;
     int64_t nbk, iu, stride;
     __device__ double2 operator()(int64_t c, int64_t q) const {
         if (q >= nbk || c >= iu) return make_double2(0.0, 0.0);
-        return W[blockIdx.z * stride + q + c * TRD_NB];
+        return W[blockIdx.z * stride + q + c * BT64];
+    }
+};
+struct BtTW_Bsum {  // b(c, q) = W(q, c) summed over ks K-split partials (partial s at (s * batch + b))
+    const double2* W;
+    int64_t nbk, iu, ks, batch;
+    __device__ double2 operator()(int64_t c, int64_t q) const {
+        if (q >= nbk || c >= iu) return make_double2(0.0, 0.0);
+        const double2* p = W + blockIdx.z * BT64 * iu + q + c * BT64;
+        double2 acc = p[0];
+        for (int64_t s = 1; s < ks; ++s) acc = cadd(acc, p[s * batch * BT64 * iu]);
+        return acc;
+    }
+};
+struct BtStoreSplit {  // partial s of batch item b at P + (s * batch + b) * stride, leading dimension BT64
+    double2* P;
+    int64_t stride, batch;
+    __device__ void operator()(int64_t s, int64_t i, int64_t j, double2 c) const {
+        P[(s * batch + blockIdx.z) * stride + i + j * BT64] = c;
     }
 };
 struct BtVa {  // a(rr, l) = V(rr, l)
@@ -401,25 +434,33 @@ struct BtXUpd {
     }
 };
 
-// zlarft (forward, columnwise) from the Gram matrix G = V^H V: T(0:i, i) = T(0:i,0:i) (-tau_i G(0:i, i))
-__global__ void k_larft(const double2* __restrict__ G, const double2* __restrict__ tau, int64_t n, int64_t j0,
-                        int64_t nbk, double2* __restrict__ T) {
+// zlarft (forward, columnwise) from the Gram matrix G = V^H V given as ks K-split partials
+// (partial s of batch item b at G + (s * batch + b) BT64^2):
+// T(0:i, i) = T(0:i, 0:i) (-tau_i G(0:i, i)), T(i, i) = tau_i.  blockDim.x = BT64, thread l owns row l.
+__global__ void k_larft(const double2* __restrict__ G, int64_t ks, int64_t batch, const double2* __restrict__ tau,
+                        int64_t n, int64_t j0, int64_t nbk, double2* __restrict__ T) {
     const int64_t b = blockIdx.x;
-    const double2* Gb = G + b * TRD_NB * TRD_NB;
-    double2* Tb = T + b * TRD_NB * TRD_NB;
+    double2* Tb = T + b * BT64 * BT64;
     const double2* tb = tau + b * n;
-    if (threadIdx.x != 0) return;
-    for (int64_t i = 0; i < TRD_NB * TRD_NB; ++i) Tb[i] = make_double2(0.0, 0.0);
+    __shared__ double2 tmp[BT64];
+    const int l = threadIdx.x;
+    for (int q = l; q < BT64 * BT64; q += blockDim.x) Tb[q] = make_double2(0.0, 0.0);
+    __syncthreads();
     for (int64_t i = 0; i < nbk; ++i) {
         const double2 ti = tb[j0 + i];
-        Tb[i + i * TRD_NB] = ti;
-        double2 tmp[TRD_NB];
-        for (int64_t l = 0; l < i; ++l) tmp[l] = cmul(cmake(-ti.x, -ti.y), Gb[l + i * TRD_NB]);
-        for (int64_t l = 0; l < i; ++l) {
-            double2 s = make_double2(0.0, 0.0);
-            for (int64_t q = l; q < i; ++q) s = cadd(s, cmul(Tb[l + q * TRD_NB], tmp[q]));
-            Tb[l + i * TRD_NB] = s;
+        if (l < i) {
+            double2 g = make_double2(0.0, 0.0);
+            for (int64_t s = 0; s < ks; ++s) g = cadd(g, G[(s * batch + b) * BT64 * BT64 + l + i * BT64]);
+            tmp[l] = cmul(cmake(-ti.x, -ti.y), g);
         }
+        __syncthreads();
+        if (l < i) {
+            double2 acc = make_double2(0.0, 0.0);
+            for (int64_t q = l; q < i; ++q) acc = cadd(acc, cmul(Tb[l + q * BT64], tmp[q]));
+            Tb[l + i * BT64] = acc;
+        }
+        if (l == 0) Tb[i + i * BT64] = ti;
+        __syncthreads();
     }
 }
 
@@ -427,28 +468,32 @@ int backtransform_fp64(cudaStream_t st, const double2* A, int64_t lda, int64_t s
                        double2* X, int64_t ldx, int64_t strideX, int64_t iu, int64_t batch, double2* Gws,
                        double2* Tws, double2* Wws, double2* W2ws) {
     const int64_t nrefl = n - 1;
-    const int64_t nblocks = (nrefl + TRD_NB - 1) / TRD_NB;
+    const int64_t nblocks = (nrefl + BT64 - 1) / BT64;
+    int64_t ksg_cap, ksw_cap;
+    bt64_split_caps(n, iu, batch, ksg_cap, ksw_cap);
     for (int64_t blk = nblocks - 1; blk >= 0; --blk) {
-        const int64_t j0 = blk * TRD_NB;
-        const int64_t nbk = (nrefl - j0 < TRD_NB) ? (nrefl - j0) : TRD_NB;
+        const int64_t j0 = blk * BT64;
+        const int64_t nbk = (nrefl - j0 < BT64) ? (nrefl - j0) : BT64;
         const int64_t K = n - j0 - 1;
         BtV v{A, lda, strideA, n, j0, nbk};
-        // G = V^H V (nbk x nbk)
-        FORGE_TRY((zgemm_launch<double2, KMAJOR, KMAJOR, false>(st, nbk, nbk, K, batch, BtGramA{v}, BtGramB{v},
-                                                                 BtStoreSmall{Gws, TRD_NB, TRD_NB * TRD_NB})));
-        k_larft<<<(unsigned)batch, 32, 0, st>>>(Gws, tau, n, j0, nbk, Tws);
+        // G = V^H V (nbk x nbk), split over K
+        const int64_t ksg = zg_ksplit_count(K, std::min<int64_t>(ksg_cap, (K + 255) / 256));
+        FORGE_TRY((zgemm_launch_splitk<double2, KMAJOR, KMAJOR>(st, nbk, nbk, K, batch, ksg, BtGramA{v},
+                                                                BtGramB{v}, BtStoreSplit{Gws, BT64 * BT64, batch})));
+        k_larft<<<(unsigned)batch, BT64, 0, st>>>(Gws, ksg, batch, tau, n, j0, nbk, Tws);
         FORGE_LAUNCH_CHECK();
-        // W = V^H X (nbk x iu)
-        FORGE_TRY((zgemm_launch<double2, KMAJOR, KMAJOR, false>(
-            st, nbk, iu, K, batch, BtGramA{v}, BtXk{X, ldx, strideX, n, j0, iu},
-            BtStoreSmall{Wws, TRD_NB, TRD_NB * iu})));
+        // W = V^H X (nbk x iu), split over K
+        const int64_t ksw = zg_ksplit_count(K, std::min<int64_t>(ksw_cap, (K + 255) / 256));
+        FORGE_TRY((zgemm_launch_splitk<double2, KMAJOR, KMAJOR>(st, nbk, iu, K, batch, ksw, BtGramA{v},
+                                                                BtXk{X, ldx, strideX, n, j0, iu},
+                                                                BtStoreSplit{Wws, BT64 * iu, batch})));
         // W2 = T W
         FORGE_TRY((zgemm_launch<double2, KMAJOR, KMAJOR, false>(
-            st, nbk, iu, nbk, batch, BtTW_A{Tws, nbk, TRD_NB * TRD_NB}, BtTW_B{Wws, nbk, iu, TRD_NB * iu},
-            BtStoreSmall{W2ws, TRD_NB, TRD_NB * iu})));
+            st, nbk, iu, nbk, batch, BtTW_A{Tws, nbk, BT64 * BT64}, BtTW_Bsum{Wws, nbk, iu, ksw, batch},
+            BtStoreSmall{W2ws, BT64, BT64 * iu})));
         // X(j0+1:, :) -= V W2
         FORGE_TRY((zgemm_launch<double2, IMAJOR, KMAJOR, false>(st, K, iu, nbk, batch, BtVa{v},
-                                                                 BtTW_B{W2ws, nbk, iu, TRD_NB * iu},
+                                                                 BtTW_B{W2ws, nbk, iu, BT64 * iu},
                                                                  BtXUpd{X, ldx, strideX, j0})));
     }
     return 0;
@@ -550,10 +595,12 @@ void carve(EigArgs& g, Carve& c) {
     g.scr = c.take<double>(4 * n * iu * B);
     g.pivs = c.take<unsigned char>(n * iu * B);
     g.fail = c.take<int>(B);
-    g.G = c.take<double2>(B * TRD_NB * TRD_NB);
-    g.T = c.take<double2>(B * TRD_NB * TRD_NB);
-    g.Wb = c.take<double2>(B * TRD_NB * iu);
-    g.W2b = c.take<double2>(B * TRD_NB * iu);
+    int64_t ksg, ksw;
+    bt64_split_caps(n, iu, B, ksg, ksw);
+    g.G = c.take<double2>(ksg * B * BT64 * BT64);
+    g.T = c.take<double2>(B * BT64 * BT64);
+    g.Wb = c.take<double2>(ksw * B * BT64 * iu);
+    g.W2b = c.take<double2>(B * BT64 * iu);
 }
 }  // namespace
 

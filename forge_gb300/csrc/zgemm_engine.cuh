@@ -39,11 +39,19 @@ __device__ __forceinline__ void zg_load_tile(V (*S)[BROWS + 1], const F& f, int6
     }
 }
 
-// Grid: x = tiles along M, y = tiles along N, z = batch (passed to the functors as blockIdx.z).
-// LOWER: skip tiles entirely above the diagonal (i < j for all elements) and elements i < j.
-template <class V, int AMAJOR, int BMAJOR, bool LOWER, class FA, class FB, class EPI>
-__global__ void __launch_bounds__(ZG_THREADS) k_zgemm(int64_t M, int64_t N, int64_t K, FA fa, FB fb, EPI epi) {
-    const int64_t i0 = (int64_t)blockIdx.x * ZG_BM, j0 = (int64_t)blockIdx.y * ZG_BN;
+// Grid: x = tiles along M (times K splits), y = tiles along N, z = batch (passed to the functors
+// as blockIdx.z).  LOWER: skip tiles entirely above the diagonal and elements i < j.
+// SPLIT: blockIdx.x = s * (M tiles) + tile; split s sums k in [s kchunk, min(K, (s+1) kchunk))
+// (kchunk a multiple of ZG_BK, so no k is summed twice) and the epilogue is called as
+// epi(s, i, j, c) with its partial sum.
+template <class V, int AMAJOR, int BMAJOR, bool LOWER, bool SPLIT, class FA, class FB, class EPI>
+__global__ void __launch_bounds__(ZG_THREADS)
+    k_zgemm(int64_t M, int64_t N, int64_t K, int64_t kchunk, FA fa, FB fb, EPI epi) {
+    const int64_t mt = (M + ZG_BM - 1) / ZG_BM;
+    const int64_t split = SPLIT ? blockIdx.x / mt : 0;
+    const int64_t i0 = (int64_t)(blockIdx.x - split * mt) * ZG_BM, j0 = (int64_t)blockIdx.y * ZG_BN;
+    const int64_t klo = SPLIT ? split * kchunk : 0;
+    const int64_t khi = SPLIT ? (K < klo + kchunk ? K : klo + kchunk) : K;
     if (LOWER && i0 + ZG_BM - 1 < j0) return;
     __shared__ V As[ZG_BK][ZG_BM + 1];
     __shared__ V Bs[ZG_BK][ZG_BN + 1];
@@ -53,7 +61,7 @@ __global__ void __launch_bounds__(ZG_THREADS) k_zgemm(int64_t M, int64_t N, int6
     for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < 4; ++b) acc[a][b] = vzero<V>();
-    for (int64_t k0 = 0; k0 < K; k0 += ZG_BK) {
+    for (int64_t k0 = klo; k0 < khi; k0 += ZG_BK) {
         zg_load_tile<AMAJOR, ZG_BM>(As, fa, i0, k0);
         zg_load_tile<BMAJOR, ZG_BN>(Bs, fb, j0, k0);
         __syncthreads();
@@ -81,7 +89,12 @@ __global__ void __launch_bounds__(ZG_THREADS) k_zgemm(int64_t M, int64_t N, int6
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             int64_t i = i0 + tx + 16 * a, j = j0 + ty + 16 * b;
-            if (i < M && j < N && (!LOWER || i >= j)) epi(i, j, acc[a][b]);
+            if (i < M && j < N && (!LOWER || i >= j)) {
+                if constexpr (SPLIT)
+                    epi(split, i, j, acc[a][b]);
+                else
+                    epi(i, j, acc[a][b]);
+            }
         }
 }
 
@@ -90,7 +103,30 @@ inline int zgemm_launch(cudaStream_t st, int64_t M, int64_t N, int64_t K, int64_
                         const FB& fb, const EPI& epi) {
     if (M <= 0 || N <= 0 || batch <= 0) return 0;
     dim3 grd((unsigned)((M + ZG_BM - 1) / ZG_BM), (unsigned)((N + ZG_BN - 1) / ZG_BN), (unsigned)batch);
-    k_zgemm<V, AMAJOR, BMAJOR, LOWER><<<grd, ZG_THREADS, 0, st>>>(M, N, K, fa, fb, epi);
+    k_zgemm<V, AMAJOR, BMAJOR, LOWER, false><<<grd, ZG_THREADS, 0, st>>>(M, N, K, K, fa, fb, epi);
+    FORGE_LAUNCH_CHECK();
+    return 0;
+}
+
+// Number of K splits zgemm_launch_splitk runs for a K extent when `want` are asked for (none empty).
+inline int64_t zg_ksplit_count(int64_t K, int64_t want) {
+    if (want <= 1 || K <= ZG_BK) return 1;
+    int64_t chunk = (K + want - 1) / want;
+    chunk = (chunk + ZG_BK - 1) / ZG_BK * ZG_BK;
+    return (K + chunk - 1) / chunk;
+}
+
+// Split-K form: ks = zg_ksplit_count(K, want) partial products, epilogue epi(s, i, j, c).
+template <class V, int AMAJOR, int BMAJOR, class FA, class FB, class EPI>
+inline int zgemm_launch_splitk(cudaStream_t st, int64_t M, int64_t N, int64_t K, int64_t batch, int64_t want,
+                               const FA& fa, const FB& fb, const EPI& epi) {
+    if (M <= 0 || N <= 0 || batch <= 0) return 0;
+    const int64_t ks = zg_ksplit_count(K, want);
+    int64_t chunk = (K + ks - 1) / ks;
+    chunk = (chunk + ZG_BK - 1) / ZG_BK * ZG_BK;
+    const int64_t mt = (M + ZG_BM - 1) / ZG_BM;
+    dim3 grd((unsigned)(mt * ks), (unsigned)((N + ZG_BN - 1) / ZG_BN), (unsigned)batch);
+    k_zgemm<V, AMAJOR, BMAJOR, false, true><<<grd, ZG_THREADS, 0, st>>>(M, N, K, chunk, fa, fb, epi);
     FORGE_LAUNCH_CHECK();
     return 0;
 }
