@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(_HERE, "libforge_gpu.so")
 
 FORGE_PREC_FP64 = 0
 FORGE_PREC_MIXED = 1
+FORGE_MIX_ODA, FORGE_MIX_PULAY = 0, 1
 FORGE_DEG_REFERENCE = 0
 FORGE_DEG_CORRECTED = 1
 
@@ -91,6 +92,7 @@ SIGNATURES = {
     "forge_gpu_field_guess": [_P, _P, _P, _P],
     "forge_gpu_scf_iteration": [_P, _P, _P],
     "forge_gpu_set_precision": [_P, _I],
+    "forge_gpu_set_mixing": [_P, _I, _I, C.c_double],
     "forge_gpu_get_setup": [_P, _P],
     "forge_gpu_synchronize": [_P],
     "forge_gpu_profile": [_P, _I],
@@ -294,6 +296,11 @@ class HartreeFock:
 
     def set_precision(self, precision: str):
         _check(self.lib.forge_gpu_set_precision(self.ctx, FORGE_PREC_MIXED if precision == "mixed" else FORGE_PREC_FP64))
+
+    def set_mixing(self, mode: str = "oda", depth: int = 6, beta: float = 0.7):
+        """SCF mixing: "oda" (the reference's OptimalStep) or "pulay" (Anderson / Pulay, `depth` steps)."""
+        _check(self.lib.forge_gpu_set_mixing(self.ctx, FORGE_MIX_PULAY if mode == "pulay" else FORGE_MIX_ODA,
+                                             depth, beta))
 
     def LongRangeInteraction(self, copy_out: bool = True) -> Optional[np.ndarray]:
         """HartreeFock.f90:14-53."""

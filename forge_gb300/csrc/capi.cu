@@ -64,6 +64,13 @@ int scf_mix(Context& c, double2* P, const double2* Pn, double* dens, double* V, 
 int scf_combine(Context& c, double2* win, const double2* bulk);
 int scf_density(Context& c, const double2* P, double* dens);
 int scf_potential(Context& c, const double* y, const double* dens, double* V);
+int scf_diis_dots(Context& c, const DiisArgs& d);
+int scf_diis_update(Context& c, const DiisArgs& d);
+int scf_diis_residual(Context& c, const double* y, const double* din, const double* dnew, double* work,
+                      ScfScalars* sc);
+int scf_diis_dens(Context& c, const double2* P, double* dens, double* work, ScfScalars* sc);
+int scf_diis_commit(Context& c, ScfScalars* sc);
+size_t scf_diis_parts();
 // mixed-precision eigen-solver (eig_mixed.cu)
 int eig_mixed(cudaStream_t st, EigArgs& g, void* mixed_ws);
 size_t eig_mixed_workspace_bytes(int64_t n, int64_t iu, int64_t batch);
@@ -83,6 +90,16 @@ struct forge_ctx {
     DevBuf projws, tcerr;  // tensor-core projector staging and its error flag
     int64_t eig_batch = 0;
     int64_t k_begin = 0, k_end = 0;  // local k range (k_end = 0: all k)
+    // mixing: FORGE_MIX_ODA (OptimalStep, the reference) or FORGE_MIX_PULAY (Anderson / Pulay)
+    int mix_mode = FORGE_MIX_ODA;
+    int diis_depth = 6;
+    double diis_beta = 0.7;
+    DevBuf diis_hist, diis_rprev, diis_part;
+    std::vector<int> diis_order;     // complete history slots, oldest first
+    int diis_pending = -1;           // slot holding dX of the last step (its dR comes next iteration)
+    int diis_nslots = 0;             // slots allocated (depth + 1)
+    bool diis_has_prev = false;
+    double diis_G[DIIS_MAX][DIIS_MAX] = {};
     bool have_solve = false, have_sort = false, have_pnew = false, have_state = false, bulk_is_fused = false;
     std::vector<int64_t> h_sorted_idx;
     std::vector<double2> h_bph;
@@ -272,6 +289,135 @@ int project_fused(forge_ctx* x) {
         }
     }
     x->have_pnew = true;
+    return 0;
+}
+
+// forget the mixing history (new state, new precision)
+void diis_reset(forge_ctx* x) {
+    x->diis_order.clear();
+    x->diis_pending = -1;
+    x->diis_has_prev = false;
+}
+
+// small dense solve G g = b (k <= DIIS_MAX), Gaussian elimination with partial pivoting
+bool diis_solve(int k, double G[DIIS_MAX][DIIS_MAX], const double* b, double* g) {
+    double A[DIIS_MAX][DIIS_MAX + 1];
+    for (int i = 0; i < k; ++i) {
+        for (int j = 0; j < k; ++j) A[i][j] = G[i][j];
+        A[i][k] = b[i];
+    }
+    for (int c = 0; c < k; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < k; ++r)
+            if (std::fabs(A[r][c]) > std::fabs(A[piv][c])) piv = r;
+        if (A[piv][c] == 0.0) return false;
+        if (piv != c)
+            for (int j = 0; j <= k; ++j) std::swap(A[c][j], A[piv][j]);
+        for (int r = c + 1; r < k; ++r) {
+            const double f = A[r][c] / A[c][c];
+            for (int j = c; j <= k; ++j) A[r][j] -= f * A[c][j];
+        }
+    }
+    for (int i = k - 1; i >= 0; --i) {
+        double t = A[i][k];
+        for (int j = i + 1; j < k; ++j) t -= A[i][j] * g[j];
+        g[i] = t / A[i][i];
+    }
+    return true;
+}
+
+// Anderson / Pulay step: x_next = x + beta r - sum_i g_i (dX_i + beta dR_i), with g minimising
+// |r - sum_i g_i dR_i| over the last `depth` (dX, dR) pairs.  c.P holds x, x->Pn holds P_new.
+int pulay_step(forge_ctx* x) {
+    Context& c = x->c;
+    const size_t nn4 = 4 * (size_t)c.N * c.N;
+    if (x->diis_nslots == 0) {
+        // as many slots as memory allows, up to depth + 1 (each slot: dX and dR, complex64)
+        size_t freeb = 0, totalb = 0;
+        cudaMemGetInfo(&freeb, &totalb);
+        const size_t slot = 2 * nn4 * sizeof(float2);
+        const size_t avail = freeb > ((size_t)6 << 30) + nn4 * sizeof(float2) ? freeb - ((size_t)6 << 30) - nn4 * sizeof(float2) : 0;
+        int ns = std::min<int>(x->diis_depth + 1, DIIS_MAX);
+        while (ns > 2 && (size_t)ns * slot > avail) --ns;
+        FORGE_TRY(x->diis_hist.ensure((size_t)ns * slot));
+        FORGE_TRY(x->diis_rprev.ensure(nn4 * sizeof(float2)));
+        FORGE_TRY(x->diis_part.ensure(scf_diis_parts() * sizeof(double)));
+        x->diis_nslots = ns;
+    }
+    DiisArgs d{};
+    d.P = c.P.as<double2>();
+    d.Pn = x->Pn.as<double2>();
+    d.hist = x->diis_hist.as<float2>();
+    d.rprev = x->diis_rprev.as<float2>();
+    d.nn4 = nn4;
+    d.beta = x->diis_beta;
+    d.part = x->diis_part.as<double>();
+    const int depth = x->diis_nslots - 1;
+    if (!x->diis_has_prev) {
+        // first step: linear mixing; its dX waits in slot 0 for the next residual
+        d.nslots = 0;
+        d.spend = 0;
+        FORGE_TRY(scf_diis_update(c, d));
+        x->diis_pending = 0;
+        x->diis_has_prev = true;
+        x->diis_order.clear();
+        return 0;
+    }
+    // complete the pending pair with dR = r - r_prev; dots with every complete pair
+    const int snew = x->diis_pending;
+    std::vector<int> list = x->diis_order;
+    list.push_back(snew);
+    d.snew = snew;
+    d.nslots = (int)list.size();
+    for (int i = 0; i < d.nslots; ++i) d.slots[i] = list[i];
+    FORGE_TRY(scf_diis_dots(c, d));
+    std::vector<double> part(scf_diis_parts());
+    FORGE_CUDA(cudaMemcpyAsync(part.data(), d.part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    double a[DIIS_MAX] = {}, bv[DIIS_MAX] = {};
+    const size_t nparts = part.size() / (2 * DIIS_MAX);
+    for (size_t q = 0; q < nparts; ++q)
+        for (int i = 0; i < d.nslots; ++i) {
+            a[i] += part[q * 2 * DIIS_MAX + i];
+            bv[i] += part[q * 2 * DIIS_MAX + DIIS_MAX + i];
+        }
+    for (int i = 0; i < d.nslots; ++i) {
+        x->diis_G[list[i]][snew] = a[i];
+        x->diis_G[snew][list[i]] = a[i];
+    }
+    double bmap[DIIS_MAX] = {};
+    for (int i = 0; i < d.nslots; ++i) bmap[list[i]] = bv[i];
+    x->diis_order.push_back(snew);
+    // keep `depth` complete pairs; the evicted slot takes the next dX
+    int spend;
+    if ((int)x->diis_order.size() > depth) {
+        spend = x->diis_order.front();
+        x->diis_order.erase(x->diis_order.begin());
+    } else {
+        spend = -1;
+        for (int sl = 0; sl < x->diis_nslots && spend < 0; ++sl)
+            if (std::find(x->diis_order.begin(), x->diis_order.end(), sl) == x->diis_order.end()) spend = sl;
+    }
+    // least squares on the complete pairs, lightly regularised
+    const int k = (int)x->diis_order.size();
+    double G[DIIS_MAX][DIIS_MAX], b[DIIS_MAX], g[DIIS_MAX] = {};
+    double gmax = 0.0;
+    for (int i = 0; i < k; ++i) gmax = std::max(gmax, x->diis_G[x->diis_order[i]][x->diis_order[i]]);
+    for (int i = 0; i < k; ++i) {
+        for (int j = 0; j < k; ++j) G[i][j] = x->diis_G[x->diis_order[i]][x->diis_order[j]];
+        G[i][i] += 1e-10 * gmax;
+        b[i] = bmap[x->diis_order[i]];
+    }
+    if (!diis_solve(k, G, b, g))
+        for (int i = 0; i < k; ++i) g[i] = 0.0;
+    d.nslots = k;
+    for (int i = 0; i < k; ++i) {
+        d.slots[i] = x->diis_order[i];
+        d.gamma[i] = g[i];
+    }
+    d.spend = spend;
+    FORGE_TRY(scf_diis_update(c, d));
+    x->diis_pending = spend;
     return 0;
 }
 
@@ -484,7 +630,27 @@ int forge_gpu_set_precision(forge_ctx* x, int64_t precision) {
     if (x->c.precision != (int)precision) {
         x->c.precision = (int)precision;
         x->eig_batch = 0;
+        diis_reset(x);   // the residual map changes with the precision
     }
+    return 0;
+}
+
+int forge_gpu_set_mixing(forge_ctx* x, int64_t mode, int64_t depth, double beta) {
+    FORGE_TRY(check_ctx(x));
+    if ((mode != FORGE_MIX_ODA && mode != FORGE_MIX_PULAY) || depth < 1 || depth > DIIS_MAX - 1 || !(beta > 0.0) ||
+        beta > 1.0) {
+        set_error(FORGE_ERR_ARG, "set_mixing: mode %lld, depth %lld (1..%d), beta %g (0..1]", (long long)mode,
+                  (long long)depth, DIIS_MAX - 1, beta);
+        return FORGE_ERR_ARG;
+    }
+    x->mix_mode = (int)mode;
+    if (x->diis_depth != (int)depth) {
+        x->diis_depth = (int)depth;
+        x->diis_nslots = 0;
+        x->diis_hist.release();
+    }
+    x->diis_beta = beta;
+    diis_reset(x);
     return 0;
 }
 
@@ -562,6 +728,7 @@ int forge_gpu_long_range(forge_ctx* x, double* LongRange) {
 
 int forge_gpu_set_state(forge_ctx* x, const double* zFock) {
     FORGE_TRY(check_ctx(x));
+    diis_reset(x);
     if (!zFock) {
         set_error(FORGE_ERR_ARG, "forge_gpu_set_state: null zFock");
         return FORGE_ERR_ARG;
@@ -911,6 +1078,7 @@ int forge_gpu_mix_potential(forge_ctx* x, double Step, double* DensityConvergenc
 
 int forge_gpu_plain_guess(forge_ctx* x, double* Energies) {
     FORGE_TRY(check_ctx(x));
+    diis_reset(x);
     Context& c = x->c;
     if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
     const size_t NN = (size_t)c.N * c.N;
@@ -929,6 +1097,7 @@ int forge_gpu_plain_guess(forge_ctx* x, double* Energies) {
 
 int forge_gpu_field_guess(forge_ctx* x, const double* zFock, double* Energies, double* residuals) {
     FORGE_TRY(check_ctx(x));
+    diis_reset(x);
     Context& c = x->c;
     if (!zFock || !residuals) {
         set_error(FORGE_ERR_ARG, "field_guess: null argument");
@@ -983,6 +1152,7 @@ int forge_gpu_field_guess(forge_ctx* x, const double* zFock, double* Energies, d
 
 int forge_gpu_prepare_state(forge_ctx* x, double* Energies) {
     FORGE_TRY(check_ctx(x));
+    diis_reset(x);
     Context& c = x->c;
     if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
     return prepare_state_device(x, Energies);
@@ -1012,9 +1182,23 @@ int forge_gpu_scf_iteration(forge_ctx* x, double* Energies, forge_iter_report* r
     FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(),
                                x->dens_new.as<double>(), x->y.as<double>(), x->work.as<double>(),
                                x->sc.as<ScfScalars>()));
-    FORGE_TRY(scf_oda(c, x->sc.as<ScfScalars>(), 0));
-    FORGE_TRY(scf_mix(c, c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(), c.V.as<double>(),
-                      x->y.as<double>(), x->work.as<double>(), x->sc.as<ScfScalars>()));
+    if (x->mix_mode == FORGE_MIX_PULAY) {
+        // residual of (P_in, P_new), then the Anderson / Pulay state, its density, potential and energies
+        ScfScalars* sc = x->sc.as<ScfScalars>();
+        FORGE_TRY(scf_diis_residual(c, x->y.as<double>(), c.dens.as<double>(), x->dens_new.as<double>(),
+                                    x->work.as<double>(), sc));
+        FORGE_TRY(pulay_step(x));
+        FORGE_TRY(scf_diis_dens(c, c.P.as<double2>(), c.dens.as<double>(), x->work.as<double>(), sc));
+        FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), c.P.as<double2>(), c.dens.as<double>(),
+                                   c.dens.as<double>(), x->y.as<double>(), x->work.as<double>(), sc));
+        FORGE_TRY(scf_potential(c, x->y.as<double>(), c.dens.as<double>(), c.V.as<double>()));
+        FORGE_TRY(scf_oda(c, sc, 1));
+        FORGE_TRY(scf_diis_commit(c, sc));
+    } else {
+        FORGE_TRY(scf_oda(c, x->sc.as<ScfScalars>(), 0));
+        FORGE_TRY(scf_mix(c, c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(), c.V.as<double>(),
+                          x->y.as<double>(), x->work.as<double>(), x->sc.as<ScfScalars>()));
+    }
     FORGE_TRY(read_scalars(x, &h));
     x->have_pnew = false;
     if (Energies)

@@ -34,7 +34,9 @@ struct EigArgs {
     int64_t scr_stride;         // >= iu
     int* fail;                  // batch
     double2 *G, *T, *Wb, *W2b;  // back-transform: NB x NB, NB x NB, NB x iu, NB x iu per batch
+    float* tf;                  // batch x 2n: FP32 copies of d and e^2 (FP32 bisection)
     double ortol_rel;
+    int bisect_f32 = 0;         // 1: FP32 bisection first, FP64 bisection from its bracket
 };
 
 // workspace sizes (bytes) for a given problem

@@ -162,6 +162,29 @@ __global__ void k_planes_to_x(const float* __restrict__ Xs, int64_t n, int64_t n
     }
 }
 
+// Unit 2-norm of every eigenvector column in FP64: the FP32 reflectors leave column norms off
+// by O(n eps_32), a systematic error that would otherwise shift the trace of the projectors.
+// One CTA (256 threads) per column.
+__global__ void __launch_bounds__(256) k_normalize_cols(double2* __restrict__ X, int64_t n, int64_t iu, int64_t ldx,
+                                                        int64_t strideX) {
+    const int64_t c = blockIdx.x, b = blockIdx.y;
+    double2* x = X + b * strideX + c * ldx;
+    double s = 0.0;
+    for (int64_t r = threadIdx.x; r < n; r += blockDim.x) s += x[r].x * x[r].x + x[r].y * x[r].y;
+    __shared__ double red[8];
+    s = warp_sum_d(s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < 8 ? red[threadIdx.x] : 0.0;
+        t = warp_sum_d(t);
+        if (threadIdx.x == 0) red[0] = t;
+    }
+    __syncthreads();
+    const double scl = red[0] > 0.0 ? 1.0 / sqrt(red[0]) : 1.0;
+    for (int64_t r = threadIdx.x; r < n; r += blockDim.x) x[r] = make_double2(x[r].x * scl, x[r].y * scl);
+}
+
 // ---------------------------------------------------------------- rank-2k update on the tensor cores
 struct Her2kStageArgs {
     const float2* A;
@@ -217,26 +240,30 @@ struct Her2kTcEpi {
     __device__ void operator()(int64_t b, int64_t row, int64_t col0, const float* v, int64_t M, int64_t N) const {
         const int64_t i = row >> 1;
         const bool even = (row & 1) == 0;
-        float im[32];
-#pragma unroll
-        for (int q = 0; q < 32; ++q) im[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
-        if (!even || row >= M) return;
         float2* __restrict__ base = A + b * strideA + (r0 + i);
-        // all 32 loads first (independent), then the updates: no load waits behind a store
-        float2 old[32];
+        // two halves of 16 columns: 16 independent loads first, then the updates
 #pragma unroll
-        for (int q = 0; q < 32; ++q) {
-            const int64_t j = col0 + q;
-            old[q] = (j < N && j <= i) ? base[(r0 + j) * lda] : make_float2(0.f, 0.f);
-        }
+        for (int h0 = 0; h0 < 32; h0 += 16) {
+            float im[16];
 #pragma unroll
-        for (int q = 0; q < 32; ++q) {
-            const int64_t j = col0 + q;
-            if (j < N && j <= i) {
-                float2 y = old[q];
-                y.x -= v[q];
-                y.y = (i == j) ? 0.f : y.y - im[q];
-                base[(r0 + j) * lda] = y;
+            for (int q = 0; q < 16; ++q) im[q] = __shfl_xor_sync(0xffffffffu, v[h0 + q], 1);
+            if (even && row < M) {
+                float2 old[16];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int64_t j = col0 + h0 + q;
+                    old[q] = (j < N && j <= i) ? base[(r0 + j) * lda] : make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int64_t j = col0 + h0 + q;
+                    if (j < N && j <= i) {
+                        float2 y = old[q];
+                        y.x -= v[h0 + q];
+                        y.y = (i == j) ? 0.f : y.y - im[q];
+                        base[(r0 + j) * lda] = y;
+                    }
+                }
             }
         }
     }
@@ -376,14 +403,14 @@ struct BtW1Epi {
     float2* W;
     int64_t nbk, iu;
     __device__ void operator()(int64_t z, int64_t row, int64_t col0, const float* v, int64_t M, int64_t N) const {
-        const int64_t b = z;   // partial index
         const int64_t l = row >> 1;
-        const bool even = (row & 1) == 0;
+        const bool keep = (row & 1) == 0 && l < nbk;
+        float2* __restrict__ w = W + z * BT_NB * iu + l + col0 * BT_NB;   // partial z
+        const int64_t nc = iu - col0;
 #pragma unroll
         for (int q = 0; q < 32; ++q) {
             const float im = __shfl_xor_sync(0xffffffffu, v[q], 1);
-            const int64_t c = col0 + q;
-            if (even && l < nbk && c < iu) W[b * BT_NB * iu + l + c * BT_NB] = make_float2(v[q], im);
+            if (keep && q < nc) w[q * BT_NB] = make_float2(v[q], im);
         }
     }
 };
@@ -437,13 +464,13 @@ struct BtXEpi {
         const bool even = (row & 1) == 0;
         const size_t P = (size_t)n4 * iu;
         float* __restrict__ X = Xs + b * 4 * P;
-        float im[32];
-#pragma unroll
-        for (int q = 0; q < 32; ++q) im[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
-        if (!even || row >= M || r >= n) return;
         // two half-chunks of 16 columns: 64 independent loads, then the re-split stores
 #pragma unroll
         for (int h0 = 0; h0 < 32; h0 += 16) {
+            float im[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) im[q] = __shfl_xor_sync(0xffffffffu, v[h0 + q], 1);
+            if (!even || row >= M || r >= n) continue;
             float hr[16], hi[16], lr[16], li[16];
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
@@ -460,7 +487,7 @@ struct BtXEpi {
                 if (c < iu) {
                     const size_t o = (size_t)c * n4 + r;
                     const float xr = (hr[q] + lr[q]) - v[h0 + q];
-                    const float xi = (hi[q] + li[q]) - im[h0 + q];
+                    const float xi = (hi[q] + li[q]) - im[q];
                     float h, l;
                     split2(xr, h, l);
                     X[o] = h;
@@ -571,7 +598,10 @@ int eig_mixed(cudaStream_t st, EigArgs& g, void* mixed_ws) {
     a.her2k_user = &ws;
     FORGE_CUDA(cudaMemsetAsync(ws.cnt, 0, sizeof(unsigned) * 4 * batch, st));
     FORGE_TRY(tridiagonalize<float>(st, a, batch));
-    FORGE_TRY(tridiag_eigvecs(st, g));
+    // eigenvalues of T: FP32 bisection, then FP64 bisection from the FP32 bracket
+    EigArgs ge = g;
+    ge.bisect_f32 = 1;
+    FORGE_TRY(tridiag_eigvecs(st, ge));
     dim3 gz((unsigned)((ws.n4 + 31) / 32), (unsigned)((iu + 31) / 32), (unsigned)batch);
     k_z_to_planes<<<gz, dim3(32, 8), 0, st>>>(g.Z, n, ws.n4, iu, ws.Xs);
     FORGE_LAUNCH_CHECK();
@@ -579,6 +609,8 @@ int eig_mixed(cudaStream_t st, EigArgs& g, void* mixed_ws) {
     FORGE_TRY(backtransform_tc(st, ws, batch));
     prof_end(ST_BACKTRANSFORM, batch * (double)n * iu * 16.0 * 2.0, batch * 3.0 * 8.0 * (double)n * n * iu);
     k_planes_to_x<<<dim3(1216, (unsigned)batch), 256, 0, st>>>(ws.Xs, n, ws.n4, iu, g.X, g.ldx, g.strideX);
+    FORGE_LAUNCH_CHECK();
+    k_normalize_cols<<<dim3((unsigned)iu, (unsigned)batch), 256, 0, st>>>(g.X, n, iu, g.ldx, g.strideX);
     FORGE_LAUNCH_CHECK();
     int herr = 0;
     FORGE_CUDA(cudaMemcpyAsync(&herr, ws.err, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -341,10 +341,14 @@ int forge_host_run_scf(forge_ctx* ctx, const forge_scf_options* opts, const doub
     bool mixed = switching;
     int64_t it = 0;
     double res = 1e300;
+    // the mixed phase also ends when its residual stalls at the FP32 noise floor: no new best
+    // (by a factor 0.8) in three iterations
+    double best = 1e300;
+    int stall = 0;
     while (it < opts->itmax) {
         ++it;
         if (mixed && ((opts->mixed_until > 0 && it > opts->mixed_until) ||
-                      (opts->mixed_switch_tol > 0.0 && res < opts->mixed_switch_tol))) {
+                      (opts->mixed_switch_tol > 0.0 && (res < opts->mixed_switch_tol || stall >= 3)))) {
             mixed = false;
             if ((rc = forge_gpu_set_precision(ctx, FORGE_PREC_FP64))) {
                 close_files();
@@ -360,6 +364,12 @@ int forge_host_run_scf(forge_ctx* ctx, const forge_scf_options* opts, const doub
         }
         if (reports) reports[it - 1] = r;
         res = r.residual;
+        if (res < 0.8 * best) {
+            best = res;
+            stall = 0;
+        } else {
+            ++stall;
+        }
         if (fc)  // Main.f90:616-623
             std::fprintf(fc, "%5.1f   %9.6f   %5.3f   %24.9f   \n", (double)it, r.DensityConvergence, r.Step,
                          r.TotalEnergyIn - r.TotalEnergy);

@@ -36,4 +36,18 @@ struct ScfScalars {
     double dn_max, dV_max, residual;
 };
 
+// Pulay / Anderson mixing (scf.cu)
+constexpr int DIIS_MAX = 8;
+struct DiisArgs {
+    double2* P;            // state x (P_in), overwritten by the mixed state
+    const double2* Pn;     // P_new
+    float2* hist;          // slots x {dX, dR} x nn4 (complex64)
+    float2* rprev;         // previous residual (complex64)
+    size_t nn4;            // 4 N^2
+    int slots[DIIS_MAX];   // history slots used
+    double gamma[DIIS_MAX];
+    int nslots, snew, spend;
+    double beta;
+    double* part;          // DIIS_CTAS x 2 x DIIS_MAX partial dots
+};
 }  // namespace forge

@@ -360,6 +360,9 @@ __global__ void k_reduce_hforms(const double* __restrict__ hpart, int nparts, Sc
 struct EnergyParams {
     double alpha, alphaH, U, StepAlternative;
     int64_t numS;
+    // mixed precision only: a step below 1 whose predicted gain over step 1, c2 (1 - s)^2, is below
+    // oda_noise |E_tot| is noise of the FP32-level P_new, and step 1 is taken (0: the reference rule)
+    double oda_noise;
 };
 
 // energies of the state (1-s) a + s b from the forms
@@ -400,6 +403,7 @@ __global__ void k_oda(ScfScalars* sc, EnergyParams p, int mode) {
         step = 1.0;
     else
         step = p.StepAlternative;
+    if (p.oda_noise > 0.0 && step < 1.0 && c2 * (1.0 - step) * (1.0 - step) < p.oda_noise * fabs(c0)) step = 1.0;
     energies_at(sc, step, Es);
     for (int t = 0; t < 4; ++t) sc->Eout[t] = Es[t];
     sc->E1tot = t1;
@@ -511,7 +515,8 @@ int scf_energy_forms(Context& c, const double* te, const double2* Pa, const doub
 size_t scf_work_doubles(int64_t N) { return RED_CTAS * 8 + (size_t)LR_CHUNKS * 2 * N + 8 * ((N + 255) / 256) + 64; }
 
 int scf_oda(Context& c, ScfScalars* sc, int mode) {
-    EnergyParams p{c.s.alpha, c.s.alphaH, c.s.U, c.s.StepAlternative, 1};
+    EnergyParams p{c.s.alpha, c.s.alphaH, c.s.U, c.s.StepAlternative, 1,
+                   c.precision == FORGE_PREC_MIXED ? 1e-8 : 0.0};
     k_oda<<<1, 32, 0, c.stream>>>(sc, p, mode);
     FORGE_LAUNCH_CHECK();
     return 0;
@@ -537,6 +542,152 @@ int scf_combine(Context& c, double2* win, const double2* bulk) {
     FORGE_LAUNCH_CHECK();
     return 0;
 }
+
+// ---------------------------------------------------------------- Pulay / Anderson mixing
+// State x = P_in (4 cells, FP64), residual r = P_new - P_in.  The history holds, per slot,
+// dX_i = x_{i+1} - x_i and dR_i = r_{i+1} - r_i in complex64: both are small near convergence, so
+// their FP32 rounding is relative to their own size; x and r themselves stay FP64.
+constexpr int DIIS_CTAS = 1216;
+
+// dR_new = (Pn - P) - rprev into slot snew; a_i = Re<dR_i, dR_new>, b_i = Re<dR_i, r> for the
+// slots in the list (snew included, with the value just stored); per-CTA partials [2 x DIIS_MAX].
+__global__ void __launch_bounds__(256) k_diis_dots(DiisArgs d) {
+    double a[DIIS_MAX], bb[DIIS_MAX];
+#pragma unroll
+    for (int i = 0; i < DIIS_MAX; ++i) a[i] = bb[i] = 0.0;
+    float2* dRnew = d.hist + (size_t)(2 * d.snew + 1) * d.nn4;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < d.nn4; q += (size_t)gridDim.x * blockDim.x) {
+        const double2 x = d.P[q], y = d.Pn[q];
+        const double rr = y.x - x.x, ri = y.y - x.y;
+        const float2 rp = d.rprev[q];
+        const float2 dn = make_float2((float)(rr - (double)rp.x), (float)(ri - (double)rp.y));
+        dRnew[q] = dn;
+#pragma unroll
+        for (int i = 0; i < DIIS_MAX; ++i) {
+            if (i < d.nslots) {
+                const float2 v = (d.slots[i] == d.snew) ? dn : d.hist[(size_t)(2 * d.slots[i] + 1) * d.nn4 + q];
+                a[i] += (double)v.x * dn.x + (double)v.y * dn.y;
+                bb[i] += (double)v.x * rr + (double)v.y * ri;
+            }
+        }
+    }
+    __shared__ double sh[32];
+#pragma unroll
+    for (int i = 0; i < DIIS_MAX; ++i) {
+        if (i < d.nslots) {   // uniform over the block
+            const double sa = block_sum(a[i], sh);
+            if (threadIdx.x == 0) d.part[(size_t)blockIdx.x * 2 * DIIS_MAX + i] = sa;
+            const double sb = block_sum(bb[i], sh);
+            if (threadIdx.x == 0) d.part[(size_t)blockIdx.x * 2 * DIIS_MAX + DIIS_MAX + i] = sb;
+        }
+    }
+}
+
+// x_next = P + beta r - sum_i g_i (dX_i + beta dR_i); dX into slot spend; rprev = r; P = x_next
+__global__ void __launch_bounds__(256) k_diis_update(DiisArgs d) {
+    float2* dXp = d.hist + (size_t)(2 * d.spend) * d.nn4;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < d.nn4; q += (size_t)gridDim.x * blockDim.x) {
+        const double2 x = d.P[q], y = d.Pn[q];
+        const double rr = y.x - x.x, ri = y.y - x.y;
+        double nx = x.x + d.beta * rr, ny = x.y + d.beta * ri;
+#pragma unroll
+        for (int i = 0; i < DIIS_MAX; ++i) {
+            if (i < d.nslots) {
+                const float2 dx = d.hist[(size_t)(2 * d.slots[i]) * d.nn4 + q];
+                const float2 dr = d.hist[(size_t)(2 * d.slots[i] + 1) * d.nn4 + q];
+                nx -= d.gamma[i] * ((double)dx.x + d.beta * (double)dr.x);
+                ny -= d.gamma[i] * ((double)dx.y + d.beta * (double)dr.y);
+            }
+        }
+        dXp[q] = make_float2((float)(nx - x.x), (float)(ny - x.y));
+        d.rprev[q] = make_float2((float)rr, (float)ri);
+        d.P[q] = make_double2(nx, ny);
+    }
+}
+
+// residual of the state before mixing: max(|V(P_new) - V(P_in)|, max alpha |fv| |P_new - P_in|),
+// from the LR products y = [LR (d_in - 1/2), LR (d_new - 1/2)] of the (P_in, P_new) energy pass
+__global__ void __launch_bounds__(256) k_diis_residual(const double* __restrict__ y, const double* __restrict__ din,
+                                                       const double* __restrict__ dnew, int64_t N, double alphaH,
+                                                       double U, double* __restrict__ mpart) {
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double dv = 0.0;
+    if (n < N) dv = fabs(2.0 * alphaH * (y[N + n] - y[n]) + U * (dnew[n] - din[n]));
+    __shared__ double sh[32];
+    const double r = block_max(dv, sh);
+    if (threadIdx.x == 0) mpart[blockIdx.x] = r;
+}
+
+// density of the mixed state and max |n - n_in|
+__global__ void __launch_bounds__(256) k_diis_dens(const double2* __restrict__ P, int64_t N, double* __restrict__ dens,
+                                                   double* __restrict__ mpart) {
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double dn = 0.0;
+    if (n < N) {
+        const double d = P[n + (size_t)n * N].x;
+        dn = fabs(d - dens[n]);
+        dens[n] = d;
+    }
+    __shared__ double sh[32];
+    const double r = block_max(dn, sh);
+    if (threadIdx.x == 0) mpart[blockIdx.x] = r;
+}
+
+__global__ void k_diis_finish(const double* __restrict__ rpart, const double* __restrict__ dpart, int nparts,
+                              ScfScalars* sc, int stage) {
+    if (threadIdx.x != 0) return;
+    double m = 0.0;
+    for (int q = 0; q < nparts; ++q) m = fmax(m, stage == 0 ? rpart[q] : dpart[q]);
+    if (stage == 0) {
+        sc->dV_max = m;
+        sc->residual = fmax(m, sc->forms[5]);
+    } else if (stage == 1) {
+        sc->dn_max = m;
+    } else {
+        for (int t = 0; t < 4; ++t) sc->Ein[t] = sc->Eout[t];
+    }
+}
+
+int scf_diis_dots(Context& c, const DiisArgs& d) {
+    k_diis_dots<<<DIIS_CTAS, 256, 0, c.stream>>>(d);
+    FORGE_LAUNCH_CHECK();
+    return 0;
+}
+
+int scf_diis_update(Context& c, const DiisArgs& d) {
+    prof_begin(ST_MIX);
+    k_diis_update<<<DIIS_CTAS, 256, 0, c.stream>>>(d);
+    FORGE_LAUNCH_CHECK();
+    prof_end(ST_MIX, (double)d.nn4 * (16.0 * 3.0 + 8.0 * 2.0 + 16.0 * d.nslots), 0.0);
+    return 0;
+}
+
+int scf_diis_residual(Context& c, const double* y, const double* din, const double* dnew, double* work,
+                      ScfScalars* sc) {
+    const unsigned nb = (unsigned)((c.N + 255) / 256);
+    k_diis_residual<<<nb, 256, 0, c.stream>>>(y, din, dnew, c.N, c.s.alphaH, c.s.U, work);
+    FORGE_LAUNCH_CHECK();
+    k_diis_finish<<<1, 32, 0, c.stream>>>(work, work, (int)nb, sc, 0);
+    FORGE_LAUNCH_CHECK();
+    return 0;
+}
+
+int scf_diis_dens(Context& c, const double2* P, double* dens, double* work, ScfScalars* sc) {
+    const unsigned nb = (unsigned)((c.N + 255) / 256);
+    k_diis_dens<<<nb, 256, 0, c.stream>>>(P, c.N, dens, work);
+    FORGE_LAUNCH_CHECK();
+    k_diis_finish<<<1, 32, 0, c.stream>>>(work, work, (int)nb, sc, 1);
+    FORGE_LAUNCH_CHECK();
+    return 0;
+}
+
+int scf_diis_commit(Context& c, ScfScalars* sc) {
+    k_diis_finish<<<1, 32, 0, c.stream>>>(nullptr, nullptr, 0, sc, 2);
+    FORGE_LAUNCH_CHECK();
+    return 0;
+}
+
+size_t scf_diis_parts() { return (size_t)DIIS_CTAS * 2 * DIIS_MAX; }
 
 int scf_density(Context& c, const double2* P, double* dens) {
     k_density<<<(unsigned)((c.N + 255) / 256), 256, 0, c.stream>>>(P, c.N, dens);

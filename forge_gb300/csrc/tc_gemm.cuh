@@ -1,13 +1,18 @@
-// tcgen05 (5th-generation tensor core) GEMM for sm_103a, TF32 inputs, FP32 accumulation in TMEM.
+// tcgen05 (5th-generation tensor core) GEMM for sm_103a, TF32 inputs, FP32 results.
 //
 //   D[b](m, n) = sum_k A[b](m, k) * B[b](n, k)        (both operands K-major, fp32 storage read as tf32)
 //
-// One CTA (128 threads) per 128 x 128 output tile:
-//   warp 0 / lane 0 : TMA producer (cp.async.bulk.tensor.3d, 128B swizzle, 3-stage ring)
-//   warp 1 / lane 0 : MMA issuer   (tcgen05.mma.cta_group::1.kind::tf32, M=128 N=128 K=8)
-//   all 4 warps     : epilogue     (tcgen05.ld.32x32b.x32 -> registers -> functor)
-// TMEM: 128 columns allocated by warp 0.  Every mbarrier wait is bounded; on timeout the
-// kernel raises an error flag, stops issuing, drains, frees its TMEM and returns.
+// One CTA (192 threads) per 128 x 64 output tile:
+//   warp 0 / lane 0 : TMA producer (cp.async.bulk.tensor.3d, 128B swizzle, 4-stage ring)
+//   warp 1 / lane 0 : MMA issuer   (tcgen05.mma.cta_group::1.kind::tf32, M=128 N=64 K=8); warp 1
+//                     also allocates and frees the TMEM
+//   warps 2..5      : accumulators (tcgen05.ld.32x32b.x32 -> FP32 registers) and epilogue
+// The tensor core's FP32 accumulation truncates (measured: an all-positive K = 8192 product comes
+// out 5.9e-5 low, linearly in K), so each K block of 32 is accumulated alone into one of two TMEM
+// buffers (64 columns each) and added into round-to-nearest FP32 registers by warps 2..5 while the
+// MMAs of the next block run in the other buffer: the residual bias is that of 4 MMAs.
+// Every mbarrier wait is bounded; on timeout the kernel raises an error flag, stops issuing,
+// drains, frees its TMEM and returns.
 //
 // Complex products run as real GEMMs over operands staged by the callers (real/imag planes,
 // and hi/lo TF32 splits for FP32-accurate results: a*b ~ ah*bh + ah*bl + al*bh).
@@ -21,11 +26,12 @@
 
 namespace forge {
 
-// 3 stages x 32 KB + barriers keeps two CTAs resident per SM (2 x 128 TMEM columns), so one
-// tile's epilogue overlaps the other's main loop.
-constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 32, TC_STAGES = 3, TC_THREADS = 128;
-constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 4;  // 16 KB per operand per stage
-constexpr int TC_SMEM = TC_STAGES * 2 * TC_TILE_BYTES + 1024 + 256;
+// 4 stages x 24 KB + barriers and 128 TMEM columns per CTA keep two CTAs resident per SM.
+constexpr int TC_BM = 128, TC_BN = 64, TC_BK = 32, TC_STAGES = 4, TC_THREADS = 192;
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 4;  // 16 KB per stage
+constexpr int TC_B_BYTES = TC_BN * TC_BK * 4;  //  8 KB per stage
+constexpr int TC_SMEM = TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + 1024 + 256;
+constexpr uint32_t TC_TMEM_COLS = 2 * TC_BN;     // two accumulation buffers
 constexpr uint32_t TC_SPIN_LIMIT = 1u << 26;     // bounded waits (>> any legitimate wait)
 
 struct TcOperand {
@@ -53,8 +59,8 @@ __host__ __device__ inline TcKMap tc_kmap_plain(int64_t K) {
     return m;
 }
 
-// Builds the 3D TMA descriptor {K, rows, planes} with a 32 x 128 box and 128B swizzle.
-int tc_make_tmap(CUtensorMap* map, const TcOperand& op, int64_t batch);
+// Builds the 3D TMA descriptor {K, rows, planes} with a 32 x box_rows box and 128B swizzle.
+int tc_make_tmap(CUtensorMap* map, const TcOperand& op, int64_t batch, int box_rows);
 
 __device__ inline uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -123,6 +129,27 @@ __device__ inline void tc_commit(uint64_t* bar) {
                  : "memory");
 }
 
+// one lane polls, the warp gets the result (tcgen05.ld needs the whole warp on the same path)
+__device__ inline bool mbar_wait_warp(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+    int ok = 0;
+    if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, abort_flag) ? 1 : 0;
+    return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
+__device__ inline void tmem_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+#pragma unroll
+    for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
+}
+
 template <class EPI>
 __global__ void __launch_bounds__(TC_THREADS, 2)
     k_tc_gemm_tf32(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int64_t M,
@@ -132,13 +159,15 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     if (lower_div > 0 && ((int64_t)blockIdx.x * TC_BM + TC_BM - 1) / lower_div < (int64_t)blockIdx.y * TC_BN) return;
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
-    float* sA = (float*)base;
-    float* sB = (float*)(base + TC_STAGES * TC_TILE_BYTES);
-    uint64_t* bars = (uint64_t*)(base + 2 * TC_STAGES * TC_TILE_BYTES);
-    uint64_t* full = bars;                  // TMA -> MMA
-    uint64_t* empty = bars + TC_STAGES;     // MMA -> TMA
-    uint64_t* accum = bars + 2 * TC_STAGES; // MMA -> epilogue
-    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * TC_STAGES + 1);
+    float* sA = (float*)base;                                      // TC_STAGES x 16 KB
+    float* sB = (float*)(base + TC_STAGES * TC_A_BYTES);           // TC_STAGES x 8 KB
+    uint64_t* bars = (uint64_t*)(base + TC_STAGES * (TC_A_BYTES + TC_B_BYTES));
+    uint64_t* full = bars;                   // TMA -> MMA
+    uint64_t* empty = bars + TC_STAGES;      // MMA -> TMA
+    uint64_t* tfull = bars + 2 * TC_STAGES;  // MMA -> accumulators (2 TMEM buffers)
+    uint64_t* tfree = tfull + 2;             // accumulators -> MMA
+    uint64_t* accum = tfree + 2;             // all MMAs issued so far are complete
+    uint32_t* tmem_slot = (uint32_t*)(accum + 1);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
     volatile int* n_issued = abort_flag + 1;    // k blocks whose TMA loads were issued
     volatile int* n_consumed = abort_flag + 2;  // k blocks consumed by the MMA issuer
@@ -156,15 +185,19 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
+        for (int t = 0; t < 2; ++t) {
+            mbar_init(&tfull[t], 1);
+            mbar_init(&tfree[t], 4);
+        }
         mbar_init(accum, 1);
         *abort_flag = 0;
         *n_issued = 0;
         *n_consumed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) {
+    if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"((uint32_t)TC_BN));
+                     "r"(TC_TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -172,90 +205,109 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    if (warp == 0 && lane == 0) {
-        // ---- TMA producer
-        for (int kb = 0; kb < nk; ++kb) {
-            const int s = kb % TC_STAGES;
-            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
-            if (kb >= TC_STAGES && !mbar_wait(&empty[s], ph ^ 1u, abort_flag)) {
-                *abort_flag = 1;
-                break;
-            }
-            if (*abort_flag) break;
-            mbar_expect_tx(&full[s], 2 * TC_TILE_BYTES);
-            {
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---- TMA producer
+            for (int kb = 0; kb < nk; ++kb) {
+                const int s = kb % TC_STAGES;
+                const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
+                if (kb >= TC_STAGES && !mbar_wait(&empty[s], ph ^ 1u, abort_flag)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                if (*abort_flag) break;
+                mbar_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
                 const int kg = kb_lo + kb;
                 const int sa = kg / ka.nkp, ra = kg - sa * ka.nkp;
                 const int sb = kg / kb_map.nkp, rb = kg - sb * kb_map.nkp;
-                tma_load_3d(sA + s * (TC_TILE_BYTES / 4), &mapA, &full[s], ka.koff + ra * TC_BK, (int32_t)m0,
+                tma_load_3d(sA + s * (TC_A_BYTES / 4), &mapA, &full[s], ka.koff + ra * TC_BK, (int32_t)m0,
                             ka.zsel[sa] + ka.zbatch * (int32_t)b);
-                tma_load_3d(sB + s * (TC_TILE_BYTES / 4), &mapB, &full[s], kb_map.koff + rb * TC_BK, (int32_t)n0,
+                tma_load_3d(sB + s * (TC_B_BYTES / 4), &mapB, &full[s], kb_map.koff + rb * TC_BK, (int32_t)n0,
                             kb_map.zsel[sb] + kb_map.zbatch * (int32_t)b);
+                *n_issued = kb + 1;
             }
-            *n_issued = kb + 1;
         }
-    } else if (warp == 1 && lane == 0) {
-        // ---- MMA issuer
-        const uint32_t idesc = tc_idesc_tf32();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---- MMA issuer: K block kb accumulates alone into TMEM buffer kb & 1
+            const uint32_t idesc = tc_idesc_tf32();
+            for (int kb = 0; kb < nk; ++kb) {
+                const int s = kb % TC_STAGES;
+                const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
+                const int buf = kb & 1, use = kb >> 1;
+                if (!mbar_wait(&full[s], ph, abort_flag)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                if (use > 0 && !mbar_wait(&tfree[buf], (uint32_t)(use - 1) & 1u, abort_flag)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a0 = smem_u32(sA + s * (TC_A_BYTES / 4)), b0 = smem_u32(sB + s * (TC_B_BYTES / 4));
+#pragma unroll
+                for (int kk = 0; kk < TC_BK / 8; ++kk) {
+                    // K = 8 tf32 = 32 bytes per MMA: advance the start address inside the 128B swizzle atom
+                    tc_mma_tf32(tmem + (uint32_t)(buf * TC_BN), umma_desc_sw128(a0 + kk * 32),
+                                umma_desc_sw128(b0 + kk * 32), idesc, kk > 0 ? 1u : 0u);
+                }
+                tc_commit(&empty[s]);   // frees the stage once these MMAs have read it
+                tc_commit(&tfull[buf]);  // the block's partial product is in TMEM
+                *n_consumed = kb + 1;
+            }
+            // arrives once every MMA issued above has completed (immediately if none was issued)
+            tc_commit(accum);
+        }
+    } else {
+        // ---- accumulators: warp w reads TMEM lanes 32 (w % 4) .. + 31 = tile rows
+        const int quarter = warp & 3;
+        const int64_t row = m0 + quarter * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16);
+        float acc[TC_BN];
+#pragma unroll
+        for (int q = 0; q < TC_BN; ++q) acc[q] = 0.f;
+        bool ok = true;
         for (int kb = 0; kb < nk; ++kb) {
-            const int s = kb % TC_STAGES;
-            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
-            if (!mbar_wait(&full[s], ph, abort_flag)) {
-                *abort_flag = 1;
+            const int buf = kb & 1, use = kb >> 1;
+            if (!mbar_wait_warp(&tfull[buf], (uint32_t)use & 1u, abort_flag)) {
+                ok = false;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a0 = smem_u32(sA + s * (TC_TILE_BYTES / 4)), b0 = smem_u32(sB + s * (TC_TILE_BYTES / 4));
 #pragma unroll
-            for (int kk = 0; kk < TC_BK / 8; ++kk) {
-                // K = 8 tf32 = 32 bytes per MMA: advance the start address inside the 128B swizzle atom
-                tc_mma_tf32(tmem, umma_desc_sw128(a0 + kk * 32), umma_desc_sw128(b0 + kk * 32), idesc,
-                            (kb > 0 || kk > 0) ? 1u : 0u);
+            for (int h = 0; h < TC_BN; h += 32) {
+                float v[32];
+                tmem_ld32(trow + (uint32_t)(buf * TC_BN + h), v);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int q = 0; q < 32; ++q) acc[h + q] += v[q];
             }
-            tc_commit(&empty[s]);  // frees the stage once these MMAs have read it
-            *n_consumed = kb + 1;
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tfree[buf]);
         }
-        // arrives once every MMA issued above has completed (immediately if none was issued)
-        tc_commit(accum);
+        // warp-uniform decision (the epilogue functors shuffle across the warp)
+        const bool failed = __shfl_sync(0xffffffffu, (!ok || *abort_flag) ? 1 : 0, 0) != 0;
+        if (failed) {
+            if (lane == 0) *abort_flag = 1;
+        } else if (nk > 0) {
+            epi((int64_t)blockIdx.z, row, n0, acc, M, N);
+            epi((int64_t)blockIdx.z, row, n0 + 32, acc + 32, M, N);
+        }
     }
-    __syncwarp();
-    // ---- epilogue: all 4 warps
-    const bool acc_ok = mbar_wait(accum, 0, abort_flag);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (!acc_ok || *abort_flag) {
-        if (threadIdx.x == 0) {
-            atomicExch(err, 1);
-            // drain: the MMAs in flight (accum) and the TMA loads issued but not consumed
-            mbar_wait(accum, 0, nullptr);
-            for (int kb = *n_consumed; kb < *n_issued; ++kb)
-                mbar_wait(&full[kb % TC_STAGES], (uint32_t)(kb / TC_STAGES) & 1u, nullptr);
-        }
-    } else if (nk > 0) {
-        const int64_t row = m0 + warp * 32 + lane;
-        for (int c0 = 0; c0 < TC_BN; c0 += 32) {
-            uint32_t r[32];
-            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                  "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-                  "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
-                  "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                : "r"(taddr));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            float v[32];
-#pragma unroll
-            for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
-            epi((int64_t)blockIdx.z, row, n0 + c0, v, M, N);
-        }
+    __syncthreads();
+    if (*abort_flag && threadIdx.x == 0) {
+        atomicExch(err, 1);
+        // drain: the MMAs in flight (accum) and the TMA loads issued but not consumed
+        mbar_wait(accum, 0, nullptr);
+        for (int kb = *n_consumed; kb < *n_issued; ++kb)
+            mbar_wait(&full[kb % TC_STAGES], (uint32_t)(kb / TC_STAGES) & 1u, nullptr);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0) {
+    if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)TC_BN));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
     }
 }
 
@@ -286,8 +338,8 @@ int tc_gemm_tf32_mapped(cudaStream_t st, const TcOperand& A, const TcKMap& ka, c
         return FORGE_ERR_ARG;
     }
     CUtensorMap ma, mb;
-    FORGE_TRY(tc_make_tmap(&ma, A, batch));
-    FORGE_TRY(tc_make_tmap(&mb, B, batch));
+    FORGE_TRY(tc_make_tmap(&ma, A, batch, TC_BM));
+    FORGE_TRY(tc_make_tmap(&mb, B, batch, TC_BN));
     static bool attr_set = false;
     if (!attr_set) {
         FORGE_CUDA(cudaFuncSetAttribute(k_tc_gemm_tf32<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));

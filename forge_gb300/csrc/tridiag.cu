@@ -14,16 +14,24 @@ __device__ inline V ldv(const V* p) {
     return *p;
 }
 
-// Block-wide sum of a double (blockDim.x == 256).
-__device__ inline double block_sum_256(double v, double* sh) {
-    v = warp_sum_d(v);
+// Block-wide sum (blockDim.x == 256) in the working precision T: the FP32 path keeps its
+// per-element arithmetic off the FP64 pipe, which runs at 1/64 of the FP32 rate on this GPU.
+template <class T>
+__device__ inline T warp_sum_t(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+template <class T>
+__device__ inline T block_sum_256(T v, T* sh) {
+    v = warp_sum_t(v);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     if (l == 0) sh[w] = v;
     __syncthreads();
-    double r = 0.0;
+    T r = (T)0;
     if (threadIdx.x < 32) {
-        r = (l < 8) ? sh[l] : 0.0;
-        r = warp_sum_d(r);
+        r = (l < 8) ? sh[l] : (T)0;
+        r = warp_sum_t(r);
     }
     __syncthreads();
     return r;  // valid in thread 0
@@ -53,14 +61,14 @@ __global__ void __launch_bounds__(TRD_ROWS) k_trd_col(TrdArgs<T> a, int64_t p, i
     V* A = a.A + b * a.strideA;
     V* W = a.W + b * (n * TRD_NB);
     __shared__ V wrow[TRD_NB], arow[TRD_NB];
-    __shared__ double sh[8];
+    __shared__ T sh[8];
     if (threadIdx.x < ii) {
         wrow[threadIdx.x] = W[col + threadIdx.x * n];
         arow[threadIdx.x] = A[col + (p + threadIdx.x) * lda];
     }
     __syncthreads();
     const int64_t r = col + (int64_t)blockIdx.x * TRD_ROWS + threadIdx.x;
-    double nrm = 0.0;
+    T nrm = (T)0;
     if (r < n) {
         V x = A[r + col * lda];
         for (int l = 0; l < ii; ++l) {
@@ -77,11 +85,11 @@ __global__ void __launch_bounds__(TRD_ROWS) k_trd_col(TrdArgs<T> a, int64_t p, i
             sc[0] = (double)x.x;
             sc[1] = (double)x.y;
         }
-        if (r >= col + 2) nrm = (double)x.x * (double)x.x + (double)x.y * (double)x.y;
+        if (r >= col + 2) nrm = x.x * x.x + x.y * x.y;
     }
-    double s = block_sum_256(nrm, sh);
+    const T s = block_sum_256(nrm, sh);
     double* part = a.part + b * a.pstride;
-    if (threadIdx.x == 0) part[blockIdx.x] = s;
+    if (threadIdx.x == 0) part[blockIdx.x] = (double)s;
     if (last_cta(a.cnt + b * 4, gridDim.x) && threadIdx.x == 0) {
         double xn2 = 0.0;
         for (unsigned q = 0; q < gridDim.x; ++q) xn2 += ((volatile double*)part)[q];
@@ -126,8 +134,9 @@ __device__ inline typename CV<T>::type trd_v(const typename CV<T>::type* A, int6
                                              double sr, double si) {
     using V = typename CV<T>::type;
     if (r == col + 1) return vmake<V>((T)1, (T)0);
-    V x = A[r + col * lda];
-    return vmake<V>((T)(x.x * sr - x.y * si), (T)(x.x * si + x.y * sr));
+    const V x = A[r + col * lda];
+    const T tr = (T)sr, ti = (T)si;
+    return vmake<V>(x.x * tr - x.y * ti, x.x * ti + x.y * tr);
 }
 
 template <class T>
@@ -140,16 +149,16 @@ __global__ void __launch_bounds__(256) k_trd_hemv(TrdArgs<T> a, int64_t p, int i
     const int64_t c0 = col + 1;
     const int64_t t = blockIdx.x;
     if (t < ntiles) {
-        // tile (bi, bj) of the trailing matrix A(c0:n, c0:n): rows [128 bi, 128 bi + 128), columns
-        // [64 bj, 64 bj + 64); row block bi holds the column blocks bj <= 2 bi + 1 (prefix bi (bi+1))
-        int64_t bi = (int64_t)((sqrt(4.0 * (double)t + 1.0) - 1.0) * 0.5);
-        while ((bi + 1) * (bi + 2) <= t) ++bi;
-        while (bi * (bi + 1) > t) --bi;
-        const int64_t bj = t - bi * (bi + 1);
+        // tile (bi, bj), bj <= bi, of the trailing matrix A(c0:n, c0:n): rows [64 bi, 64 bi + 64),
+        // columns [64 bj, 64 bj + 64); t = bi (bi + 1) / 2 + bj
+        int64_t bi = (int64_t)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);   // corrected below
+        while ((bi + 1) * (bi + 2) / 2 <= t) ++bi;
+        while (bi * (bi + 1) / 2 > t) --bi;
+        const int64_t bj = t - bi * (bi + 1) / 2;
         const int64_t R0 = c0 + bi * HV_RB, C0 = c0 + bj * HV_CB;
         __shared__ V vr[HV_RB], vc[HV_CB];
         __shared__ V rsum[4][HV_RB];
-        __shared__ V cs[64][HV_CB + 1];
+        __shared__ V cs[HV_RB][HV_CB + 1];
         __shared__ V cq[4][HV_CB];
         if (threadIdx.x < HV_RB) {
             const int64_t r = R0 + threadIdx.x;
@@ -159,43 +168,36 @@ __global__ void __launch_bounds__(256) k_trd_hemv(TrdArgs<T> a, int64_t p, int i
             vc[threadIdx.x - HV_RB] = (c < n) ? trd_v<T>(A, lda, col, c, sr, si) : vzero<V>();
         }
         const int tr = threadIdx.x & 63, tg = threadIdx.x >> 6;
-        const int64_t r0 = R0 + tr, r1 = R0 + 64 + tr;
-        // 32 loads per thread (rows r0 and r1, 16 columns) issued before any arithmetic
-        V a0[16], a1[16];
+        const int64_t r0 = R0 + tr;
+        // 16 loads per thread (row r0, 16 columns) issued before any arithmetic
+        V a0[16];
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
             const int64_t c = C0 + tg * 16 + q;
             a0[q] = (r0 < n && c < n && c <= r0) ? A[r0 + c * lda] : vzero<V>();
-            a1[q] = (r1 < n && c < n && c <= r1) ? A[r1 + c * lda] : vzero<V>();
         }
         __syncthreads();
-        V racc0 = vzero<V>(), racc1 = vzero<V>();
-        const V v0 = vr[tr], v1 = vr[64 + tr];
+        V racc = vzero<V>();
+        const V v0 = vr[tr];
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
             const int64_t c = C0 + tg * 16 + q;
-            V x0 = a0[q], x1 = a1[q];
-            const bool d0 = (c == r0), d1 = (c == r1);
+            V x0 = a0[q];
+            const bool d0 = (c == r0);
             if (d0) x0.y = 0;
-            if (d1) x1.y = 0;
-            const V vcq = vc[tg * 16 + q];
-            racc0 = vadd(racc0, vmul(x0, vcq));
-            racc1 = vadd(racc1, vmul(x1, vcq));
+            racc = vadd(racc, vmul(x0, vc[tg * 16 + q]));
             // column part: conj(A(r, c)) v_r for r > c (the diagonal belongs to the row part only)
-            V s = d0 ? vzero<V>() : vcjmul(x0, v0);
-            if (!d1) s = vadd(s, vcjmul(x1, v1));
-            cs[tr][tg * 16 + q] = s;
+            cs[tr][tg * 16 + q] = d0 ? vzero<V>() : vcjmul(x0, v0);
         }
-        rsum[tg][tr] = racc0;
-        rsum[tg][64 + tr] = racc1;
+        rsum[tg][tr] = racc;
         __syncthreads();
         {
-            // column sums: thread (col, quarter of the 64 row pairs)
+            // column sums: thread (col, quarter of the 64 rows)
             const int c = threadIdx.x & 63, qt = threadIdx.x >> 6;
-            V s = vzero<V>();
+            V acc = vzero<V>();
 #pragma unroll
-            for (int i = 0; i < 16; ++i) s = vadd(s, cs[qt * 16 + i][c]);
-            cq[qt][c] = s;
+            for (int i = 0; i < 16; ++i) acc = vadd(acc, cs[qt * 16 + i][c]);
+            cq[qt][c] = acc;
         }
         __syncthreads();
         V* Yrow = a.Yrow + b * a.ystride;
@@ -258,7 +260,7 @@ __global__ void __launch_bounds__(TRD_ROWS) k_trd_finish(TrdArgs<T> a, int64_t p
     const V tau = vmake<V>((T)sc[4], (T)sc[5]);
     const int64_t c0 = col + 1;
     __shared__ V s1[TRD_NB], s2[TRD_NB];
-    __shared__ double sh[8];
+    __shared__ T sh[8];
     if (threadIdx.x < ii) {
         const V* S = a.Spart + b * a.sstride;
         V x1 = vzero<V>(), x2 = vzero<V>();
@@ -284,7 +286,7 @@ __global__ void __launch_bounds__(TRD_ROWS) k_trd_finish(TrdArgs<T> a, int64_t p
         ysl[sl][rr] = y;
     }
     __syncthreads();
-    double dre = 0.0, dim = 0.0;
+    T dre = (T)0, dim = (T)0;
     if (sl == 0 && r < n) {
         V y = vzero<V>();
 #pragma unroll
@@ -299,15 +301,15 @@ __global__ void __launch_bounds__(TRD_ROWS) k_trd_finish(TrdArgs<T> a, int64_t p
         W[r + ii * n] = y;
         // zdotc(w, v) = sum conj(w) v
         V cv = vcjmul(y, v);
-        dre = (double)cv.x;
-        dim = (double)cv.y;
+        dre = cv.x;
+        dim = cv.y;
     }
-    double s_re = block_sum_256(dre, sh);
-    double s_im = block_sum_256(dim, sh);
+    const T s_re = block_sum_256(dre, sh);
+    const T s_im = block_sum_256(dim, sh);
     double* part = a.part + b * a.pstride;
     if (threadIdx.x == 0) {
-        part[2 * blockIdx.x] = s_re;
-        part[2 * blockIdx.x + 1] = s_im;
+        part[2 * blockIdx.x] = (double)s_re;
+        part[2 * blockIdx.x + 1] = (double)s_im;
     }
     if (last_cta(a.cnt + b * 4 + 1, gridDim.x) && threadIdx.x == 0) {
         double xr = 0.0, xi = 0.0;
@@ -401,9 +403,8 @@ int tridiagonalize(cudaStream_t st, TrdArgs<T>& a, int64_t batch) {
             if (!has_refl) continue;
             ++nrefl;
             const int64_t n2 = n - col - 1;
-            const int64_t nbr = (n2 + HV_RB - 1) / HV_RB;   // 128-row blocks
-            const int64_t nbc = (n2 + HV_CB - 1) / HV_CB;   // 64-column blocks (nbc <= 2 nbr)
-            const int64_t ntiles = (nbr - 1) * nbr + nbc;   // row block bi holds min(2 bi + 2, nbc) tiles
+            const int64_t nbr = (n2 + HV_RB - 1) / HV_RB;   // 64-row blocks (= 64-column blocks)
+            const int64_t ntiles = nbr * (nbr + 1) / 2;     // row block bi holds bi + 1 tiles
             const int64_t nrb = (n2 + 255) / 256;
             dim3 gb((unsigned)(ntiles + (ii > 0 ? nrb : 0)), (unsigned)batch);
             prof_begin(ST_HEMV);

@@ -22,7 +22,7 @@ namespace forge {
 
 constexpr int TRD_NB = 32;      // panel width
 constexpr int TRD_TILE = 64;    // column granularity of the hemv partial slots (Yrow / Ycol)
-constexpr int HV_RB = 128;      // hemv tile rows
+constexpr int HV_RB = 64;       // hemv tile rows
 constexpr int HV_CB = 64;       // hemv tile columns
 constexpr int TRD_ROWS = 256;   // rows per CTA in the column kernels
 

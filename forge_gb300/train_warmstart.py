@@ -35,9 +35,9 @@ SYSTEMS = [
 QUICK = [(8, 2, 6, 2.0, 10.0), (8, 2, 6, 0.0, 10.0), (12, 2, 4, 2.0, 10.0)]
 
 
-def converge(m, L, numk, nu, eps, tol=1e-5, itmax=60):
+def converge(m, L, numk, nu, eps, tol=1e-5, itmax=60, degfactor="corrected"):
     S = fg.Setup(ntheta=m, nlayers=L, RotateLayers=(-1, 1, -1)[:L], numk=numk, nfilling=nu, epsilon=eps,
-                 precision="mixed")
+                 degfactor_mode=degfactor, precision="mixed")
     hf = fg.HartreeFock(S)
     hf.LongRangeInteraction(copy_out=False)
     hf.set_precision("mixed")
@@ -56,11 +56,13 @@ def main():
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--out", default=wsm.WEIGHTS)
     ap.add_argument("--epochs", type=int, default=80)
+    ap.add_argument("--degfactor", default="corrected", choices=["corrected", "reference"],
+                    help="occupation weight of the partially filled states used for the training SCFs")
     args = ap.parse_args()
     samples, log = [], []
     for (m, L, numk, nu, eps) in (QUICK if args.quick else SYSTEMS):
         t = time.time()
-        S, hf, P, dens, n, res = converge(m, L, numk, nu, eps)
+        S, hf, P, dens, n, res = converge(m, L, numk, nu, eps, degfactor=args.degfactor)
         samples.append(wsm.training_samples(S, hf.geometry, P, dens))
         hf.close()
         log.append(dict(m=m, nlayers=L, numk=numk, nu=nu, eps=eps, iters=n, residual=res, s=time.time() - t))

@@ -41,6 +41,8 @@ enum {
 };
 
 enum { FORGE_PREC_FP64 = 0, FORGE_PREC_MIXED = 1 };
+/* SCF mixing: the reference's OptimalStep (ODA) or Anderson / Pulay mixing of the density matrix. */
+enum { FORGE_MIX_ODA = 0, FORGE_MIX_PULAY = 1 };
 enum { FORGE_DEG_REFERENCE = 0, FORGE_DEG_CORRECTED = 1 };
 
 /* Runtime mirror of Setup.f90:6-74 (only the parameters the SCF path reads). */
@@ -187,6 +189,16 @@ int forge_gpu_prepare_state(forge_ctx* ctx, double* Energies);
 /* One full SCF iteration (Main.f90:365-595) with all arrays device-resident.
  * Energies[4] as in optimal_step (in: current, out: new). */
 int forge_gpu_scf_iteration(forge_ctx* ctx, double* Energies, forge_iter_report* report);
+
+/* Mixing of forge_gpu_scf_iteration (no counterpart in the reference, which mixes with OptimalStep
+ * only; the Anderson / Pulay option follows the benchmark description's "Pulay mixing depth 6"):
+ * FORGE_MIX_ODA (default) or FORGE_MIX_PULAY with `depth` (1..7) previous steps and mixing weight
+ * beta (0..1]: P_in <- P_in + beta r - sum_i g_i (dP_i + beta dr_i), r = P_new - P_in, with g
+ * minimising |r - sum_i g_i dr_i|.  The history (complex64 differences, 2 x 4 N^2 x 8 bytes per
+ * step) is kept on the device and is cleared by set_state, plain_guess, field_guess,
+ * prepare_state and a change of precision.  With Pulay the reported residual is that of
+ * (P_in, P_new) and Step is 1. */
+int forge_gpu_set_mixing(forge_ctx* ctx, int64_t mode, int64_t depth, double beta);
 
 /* Selects FORGE_PREC_FP64 or FORGE_PREC_MIXED for subsequent solves. */
 int forge_gpu_set_precision(forge_ctx* ctx, int64_t precision);

@@ -43,3 +43,33 @@ def test_fast_scf_converges_to_oracle_fixed_point(lib, m, numk, nu):
     assert np.max(np.abs(P - ref["P"])) <= 1e-8
     assert abs(res["TotalEnergy"] - ref["Etot"]) / so.ndim <= 1e-7
     assert np.max(np.abs(V - ref["V"])) <= 1e-7
+
+
+@pytest.mark.parametrize("precision_switch", [0.0, 1e-4])
+def test_pulay_mixing_reaches_the_oracle_fixed_point(lib, precision_switch):
+    """Anderson / Pulay mixing (forge_gpu_set_mixing) converges to the fixed point the oracle's
+    OptimalStep SCF reaches, in FP64 and in the fast (mixed, then FP64) configuration."""
+    import forge_gb300 as fg
+    m, numk, nu = 2, 3, 2.0
+    so = fo.Setup(ntheta=m, numk=numk, nfilling=nu)
+    ref = fo.run_scf(so, itmax=400, residual_tol=1e-11)
+    S = fg.Setup(ntheta=m, numk=numk, nfilling=nu)
+    with fg.HartreeFock(S) as hf:
+        hf.LongRangeInteraction(copy_out=False)
+        hf.set_mixing("pulay", depth=6, beta=0.7)
+        res, reps = hf.RunScf(itmax=200, residual_tol=1e-11, mixed_switch_tol=precision_switch)
+        P, dens, V = hf.GetState()
+    assert res["converged"]
+    assert all(r["Step"] == 1.0 for r in reps)
+    P = np.moveaxis(P, 2, 0)
+    assert np.max(np.abs(P - ref["P"])) <= 1e-8
+    assert abs(res["TotalEnergy"] - ref["Etot"]) / so.ndim <= 1e-7
+
+
+def test_set_mixing_rejects_bad_arguments(lib):
+    import forge_gb300 as fg
+    with fg.HartreeFock(fg.Setup(ntheta=2, numk=1)) as hf:
+        with pytest.raises(fg.ForgeError):
+            hf.set_mixing("pulay", depth=0)
+        with pytest.raises(fg.ForgeError):
+            hf.set_mixing("pulay", depth=6, beta=1.5)
