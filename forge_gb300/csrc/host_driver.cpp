@@ -341,14 +341,15 @@ int forge_host_run_scf(forge_ctx* ctx, const forge_scf_options* opts, const doub
     bool mixed = switching;
     int64_t it = 0;
     double res = 1e300;
-    // the mixed phase also ends when its residual stalls at the FP32 noise floor: no new best
-    // (by a factor 0.8) in three iterations
+    // the mixed phase also ends when its residual stalls near the FP32 noise floor: no new best
+    // (by a factor 0.8) in three iterations while within 100x the switch tolerance
     double best = 1e300;
     int stall = 0;
     while (it < opts->itmax) {
         ++it;
         if (mixed && ((opts->mixed_until > 0 && it > opts->mixed_until) ||
-                      (opts->mixed_switch_tol > 0.0 && (res < opts->mixed_switch_tol || stall >= 3)))) {
+                      (opts->mixed_switch_tol > 0.0 &&
+                       (res < opts->mixed_switch_tol || (stall >= 3 && res < 100.0 * opts->mixed_switch_tol))))) {
             mixed = false;
             if ((rc = forge_gpu_set_precision(ctx, FORGE_PREC_FP64))) {
                 close_files();
