@@ -236,6 +236,9 @@ def run_ours(args, cfg, rank):
         converged = bool(record.get("converged", False))
         source = ("iteration counts" + ("" if "fp64" in mean_by_prec or n_fp64 == 0 else " and FP64 iteration time")
                   + " from the recorded --converge run (profiles/scf_records.json); per-iteration times of this run")
+        if not converged:
+            source += ("; the recorded run did NOT reach the tolerance, so value is a lower bound of the "
+                       "time-to-SCF: " + str(record.get("note", "")))
     # e2e: the reference-facing per-iteration calls with host buffers (pinned), copies included
     e2e_ms = []
     N, Nk, numb = hf.N, hf.Nk, hf.numb

@@ -233,37 +233,37 @@ __global__ void k_stage_her2k(Her2kStageArgs s) {
     rb[256 + l] = zrh;  rb[320 + l] = zih;
 }
 
-// epilogue: interleaved rows (2i = Re, 2i+1 = Im) of C = U Z^H; A22(i,j) -= C(i,j) for j <= i
+// epilogue: interleaved rows (2i = Re, 2i+1 = Im) of C = U Z^H; A22(i,j) -= C(i,j) for j <= i.
+// The two lanes of a row pair split the 32 columns: the even lane updates columns 0..15, the odd
+// lane 16..31, each with 16 independent loads issued before its stores.
 struct Her2kTcEpi {
     float2* A;
     int64_t lda, strideA, r0;
     __device__ void operator()(int64_t b, int64_t row, int64_t col0, const float* v, int64_t M, int64_t N) const {
         const int64_t i = row >> 1;
-        const bool even = (row & 1) == 0;
+        const bool odd = (row & 1) != 0;
+        float other[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) other[q] = __shfl_xor_sync(0xffffffffu, odd ? v[q] : v[16 + q], 1);
+        if (row >= M) return;
+        const int h0 = odd ? 16 : 0;
         float2* __restrict__ base = A + b * strideA + (r0 + i);
-        // two halves of 16 columns: 16 independent loads first, then the updates
+        float2 old[16];
 #pragma unroll
-        for (int h0 = 0; h0 < 32; h0 += 16) {
-            float im[16];
+        for (int q = 0; q < 16; ++q) {
+            const int64_t j = col0 + h0 + q;
+            old[q] = (j < N && j <= i) ? base[(r0 + j) * lda] : make_float2(0.f, 0.f);
+        }
 #pragma unroll
-            for (int q = 0; q < 16; ++q) im[q] = __shfl_xor_sync(0xffffffffu, v[h0 + q], 1);
-            if (even && row < M) {
-                float2 old[16];
-#pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    const int64_t j = col0 + h0 + q;
-                    old[q] = (j < N && j <= i) ? base[(r0 + j) * lda] : make_float2(0.f, 0.f);
-                }
-#pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    const int64_t j = col0 + h0 + q;
-                    if (j < N && j <= i) {
-                        float2 y = old[q];
-                        y.x -= v[h0 + q];
-                        y.y = (i == j) ? 0.f : y.y - im[q];
-                        base[(r0 + j) * lda] = y;
-                    }
-                }
+        for (int q = 0; q < 16; ++q) {
+            const int64_t j = col0 + h0 + q;
+            if (j < N && j <= i) {
+                const float re = odd ? other[q] : v[q];
+                const float im = odd ? v[16 + q] : other[q];
+                float2 y = old[q];
+                y.x -= re;
+                y.y = (i == j) ? 0.f : y.y - im;
+                base[(r0 + j) * lda] = y;
             }
         }
     }
@@ -455,47 +455,47 @@ __global__ void k_stage_bt3(const float2* __restrict__ W2, int64_t iu, float* __
     o[256 + l] = rh; o[320 + l] = ih;
 }
 
-// GEMM2 epilogue: X(j0 + rr, c) -= D, re-split into the hi / lo planes
+// GEMM2 epilogue: X(j0 + rr, c) -= D, re-split into the hi / lo planes.  The two lanes of a row
+// pair split the 32 columns (even lane 0..15, odd lane 16..31).
 struct BtXEpi {
     float* Xs;
     int64_t n4, iu, j0, n;
     __device__ void operator()(int64_t b, int64_t row, int64_t col0, const float* v, int64_t M, int64_t N) const {
         const int64_t rr = row >> 1, r = j0 + rr;
-        const bool even = (row & 1) == 0;
+        const bool odd = (row & 1) != 0;
         const size_t P = (size_t)n4 * iu;
         float* __restrict__ X = Xs + b * 4 * P;
-        // two half-chunks of 16 columns: 64 independent loads, then the re-split stores
+        float other[16];
 #pragma unroll
-        for (int h0 = 0; h0 < 32; h0 += 16) {
-            float im[16];
+        for (int q = 0; q < 16; ++q) other[q] = __shfl_xor_sync(0xffffffffu, odd ? v[q] : v[16 + q], 1);
+        if (row >= M || r >= n) return;
+        const int h0 = odd ? 16 : 0;
+        float hr[16], hi[16], lr[16], li[16];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) im[q] = __shfl_xor_sync(0xffffffffu, v[h0 + q], 1);
-            if (!even || row >= M || r >= n) continue;
-            float hr[16], hi[16], lr[16], li[16];
+        for (int q = 0; q < 16; ++q) {
+            const int64_t c = col0 + h0 + q;
+            const size_t o = (size_t)(c < iu ? c : 0) * n4 + r;
+            hr[q] = X[o];
+            hi[q] = X[P + o];
+            lr[q] = X[2 * P + o];
+            li[q] = X[3 * P + o];
+        }
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int64_t c = col0 + h0 + q;
-                const size_t o = (size_t)(c < iu ? c : 0) * n4 + r;
-                hr[q] = X[o];
-                hi[q] = X[P + o];
-                lr[q] = X[2 * P + o];
-                li[q] = X[3 * P + o];
-            }
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int64_t c = col0 + h0 + q;
-                if (c < iu) {
-                    const size_t o = (size_t)c * n4 + r;
-                    const float xr = (hr[q] + lr[q]) - v[h0 + q];
-                    const float xi = (hi[q] + li[q]) - im[q];
-                    float h, l;
-                    split2(xr, h, l);
-                    X[o] = h;
-                    X[2 * P + o] = l;
-                    split2(xi, h, l);
-                    X[P + o] = h;
-                    X[3 * P + o] = l;
-                }
+        for (int q = 0; q < 16; ++q) {
+            const int64_t c = col0 + h0 + q;
+            if (c < iu) {
+                const float dre = odd ? other[q] : v[q];
+                const float dim = odd ? v[16 + q] : other[q];
+                const size_t o = (size_t)c * n4 + r;
+                const float xr = (hr[q] + lr[q]) - dre;
+                const float xi = (hi[q] + li[q]) - dim;
+                float h, l;
+                split2(xr, h, l);
+                X[o] = h;
+                X[2 * P + o] = l;
+                split2(xi, h, l);
+                X[P + o] = h;
+                X[3 * P + o] = l;
             }
         }
     }

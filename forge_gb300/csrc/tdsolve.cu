@@ -612,7 +612,9 @@ int tridiag_eigvecs(cudaStream_t st, EigArgs& g) {
         k_bisect_f32<<<gb, 128, 0, st>>>(g.tf, n, iu, g.info, g.w);
         FORGE_LAUNCH_CHECK();
     }
-    k_bisect<<<gb, 128, 0, st>>>(g.d, g.e, n, iu, g.info, g.w, g.bisect_f32, g.bisect_f32 ? 1e-10 : 0.0);
+    // full FP64 accuracy in both paths: inverse iteration on tight clusters needs it (a 1e-10 ||T||
+    // stop made the batched inverse iteration 7x slower on the twisted-bilayer spectra)
+    k_bisect<<<gb, 128, 0, st>>>(g.d, g.e, n, iu, g.info, g.w, g.bisect_f32, 0.0);
     FORGE_LAUNCH_CHECK();
     prof_end(ST_BISECT, batch * 16.0 * n, batch * 10.0 * 60.0 * (double)n * iu);
     k_clusters<<<(unsigned)batch, 32, 0, st>>>(g.w, iu, g.info, g.ortol_rel, g.clus);

@@ -285,16 +285,22 @@ __global__ void __launch_bounds__(TRD_ROWS) k_trd_finish(TrdArgs<T> a, int64_t p
         for (int64_t q = Br + sl; q < nb2; q += 8) y = vadd(y, Ycol[q * n + r]);
         ysl[sl][rr] = y;
     }
+    __syncthreads();   // s1, s2 and the slot sums are in shared memory
+    if (r < n) {
+        // the panel corrections -V s1 - W s2, split over the 8 slices
+        V y = ysl[sl][rr];
+        for (int l = sl; l < ii; l += 8) {
+            y = vsub(y, vmul(A[r + (p + l) * lda], s1[l]));
+            y = vsub(y, vmul(W[r + l * n], s2[l]));
+        }
+        ysl[sl][rr] = y;
+    }
     __syncthreads();
     T dre = (T)0, dim = (T)0;
     if (sl == 0 && r < n) {
         V y = vzero<V>();
 #pragma unroll
         for (int q = 0; q < 8; ++q) y = vadd(y, ysl[q][rr]);
-        for (int l = 0; l < ii; ++l) {
-            y = vsub(y, vmul(A[r + (p + l) * lda], s1[l]));
-            y = vsub(y, vmul(W[r + l * n], s2[l]));
-        }
         y = vmul(tau, y);
         V v = trd_v<T>(A, lda, col, r, sr, si);
         A[r + col * lda] = v;
