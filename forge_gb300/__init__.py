@@ -5,7 +5,9 @@ C-ABI of ``include/forge_gpu.h``); this package is the thin Python host that
 binds it with ctypes.  Build with ``forge_gb300.build.build()``.
 """
 from .api import (FORGE_DEG_CORRECTED, FORGE_DEG_REFERENCE, FORGE_PREC_FP64, FORGE_PREC_MIXED, ForgeError,
-                  Geometry, HartreeFock, Setup, build_geometry, load_library, parameters_string)
+                  Geometry, HartreeFock, Setup, build_geometry, load_library, parameters_string, read_fock,
+                  write_fock)
 
 __all__ = ["Setup", "Geometry", "HartreeFock", "build_geometry", "load_library", "parameters_string", "ForgeError",
+           "read_fock", "write_fock",
            "FORGE_PREC_FP64", "FORGE_PREC_MIXED", "FORGE_DEG_REFERENCE", "FORGE_DEG_CORRECTED"]

@@ -113,6 +113,8 @@ SIGNATURES = {
     "forge_host_run_scf": [_P, _P, _P, _P, _P],
     "forge_host_parameters_string": [_P, C.c_char_p, C.c_char_p, _I],
     "forge_host_plot_bands": [_P, _P, _D, _P, _P, _P, C.c_char_p],
+    "forge_host_write_fock": [_P, _P, C.c_char_p, _I],
+    "forge_host_read_fock": [_P, _P, C.c_char_p, _I],
 }
 
 _LIB = None
@@ -242,6 +244,21 @@ def plot_bands(setup: Setup, geometry: Geometry, Bands: np.ndarray, FermiEnergy:
                                                  _ptr(_f(geometry.nMomentaFlattened, np.int64)),
                                                  _ptr(np.ascontiguousarray(geometry.g1)),
                                                  _ptr(np.ascontiguousarray(geometry.g12)), path.encode()))
+
+
+def write_fock(setup: Setup, zFock: np.ndarray, path: str, record_bytes: int = 16) -> None:
+    """Fock checkpoint file of Main.f90:647-672 (record_bytes 16: gfortran recl units, 64: ifort's)."""
+    s = setup.to_struct()
+    _check(load_library().forge_host_write_fock(C.byref(s), _ptr(_f(zFock, np.complex128)), path.encode(),
+                                                record_bytes))
+
+
+def read_fock(setup: Setup, path: str, record_bytes: int = 16) -> np.ndarray:
+    """zFock (ndim, ndim, numNeighborCells) from a Fock checkpoint file (Main.f90:202-234)."""
+    s = setup.to_struct()
+    P = np.zeros((s.ndim, s.ndim, s.numNeighborCells), dtype=np.complex128, order="F")
+    _check(load_library().forge_host_read_fock(C.byref(s), _ptr(P), path.encode(), record_bytes))
+    return P
 
 
 def parameters_string(setup: Setup, statename: str = "SSS") -> str:

@@ -299,6 +299,65 @@ int forge_host_parameters_string(const forge_setup* s, const char* statename, ch
     return 0;
 }
 
+// Fock checkpoint (Main.f90:647-672, 202-234): one complex value per fixed-length record
+int forge_host_write_fock(const forge_setup* s, const double* zFock, const char* path, int64_t record_bytes) {
+    if (!s || !zFock || !path || record_bytes < 16) return FORGE_ERR_ARG;
+    const int64_t N = s->ndim, NC = s->numNeighborCells;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return FORGE_ERR_ARG;
+    std::vector<unsigned char> row((size_t)N * record_bytes, 0);
+    const size_t NN = (size_t)N * N;
+    auto put = [&](int64_t slot, int64_t i, int64_t j, int64_t m) {
+        const double* z = zFock + 2 * (m * NN + (size_t)i + (size_t)j * N);
+        std::memcpy(row.data() + slot * record_bytes, z, 16);
+    };
+    bool ok = true;
+    for (int64_t i = 0; i < N && ok; ++i) {  // R = 0: lower triangle, row i, columns 0..i
+        for (int64_t j = 0; j <= i; ++j) put(j, i, j, 0);
+        ok = std::fwrite(row.data(), (size_t)record_bytes, (size_t)(i + 1), f) == (size_t)(i + 1);
+    }
+    for (int64_t m = 1; m < NC && ok; ++m)
+        for (int64_t i = 0; i < N && ok; ++i) {
+            for (int64_t j = 0; j < N; ++j) put(j, i, j, m);
+            ok = std::fwrite(row.data(), (size_t)record_bytes, (size_t)N, f) == (size_t)N;
+        }
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? 0 : FORGE_ERR_ARG;
+}
+
+int forge_host_read_fock(const forge_setup* s, double* zFock, const char* path, int64_t record_bytes) {
+    if (!s || !zFock || !path || record_bytes < 16) return FORGE_ERR_ARG;
+    const int64_t N = s->ndim, NC = s->numNeighborCells;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return FORGE_ERR_ARG;
+    std::vector<unsigned char> row((size_t)N * record_bytes);
+    const size_t NN = (size_t)N * N;
+    bool ok = true;
+    for (int64_t i = 0; i < N && ok; ++i) {
+        ok = std::fread(row.data(), (size_t)record_bytes, (size_t)(i + 1), f) == (size_t)(i + 1);
+        for (int64_t j = 0; j <= i && ok; ++j) {
+            double z[2];
+            std::memcpy(z, row.data() + j * record_bytes, 16);
+            double* a = zFock + 2 * ((size_t)i + (size_t)j * N);
+            a[0] = z[0];
+            a[1] = z[1];
+            if (j < i) {  // zFock(j, i, 1) = conjg(zinput)
+                double* c = zFock + 2 * ((size_t)j + (size_t)i * N);
+                c[0] = z[0];
+                c[1] = -z[1];
+            }
+        }
+    }
+    for (int64_t m = 1; m < NC && ok; ++m)
+        for (int64_t i = 0; i < N && ok; ++i) {
+            ok = std::fread(row.data(), (size_t)record_bytes, (size_t)N, f) == (size_t)N;
+            for (int64_t j = 0; j < N && ok; ++j)
+                std::memcpy(zFock + 2 * (m * NN + (size_t)i + (size_t)j * N), row.data() + j * record_bytes, 16);
+        }
+    std::fclose(f);
+    return ok ? 0 : FORGE_ERR_ARG;
+}
+
 int forge_host_run_scf(forge_ctx* ctx, const forge_scf_options* opts, const double* zFock_init,
                        forge_scf_result* result, forge_iter_report* reports) {
     if (!ctx || !opts || !result) return FORGE_ERR_ARG;

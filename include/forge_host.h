@@ -63,6 +63,17 @@ int forge_host_run_scf(forge_ctx* ctx, const forge_scf_options* opts, const doub
 int forge_host_plot_bands(const forge_setup* s, const double* Bands, double FermiEnergy,
                           const int64_t* nMomentaFlattened, const double* g1, const double* g12, const char* path);
 
+/* Fock checkpoint files (Main.f90:647-672 write, Main.f90:202-234 read): a direct-access
+ * unformatted file of one complex(dp) value per record: R = 0 as the lower triangle row by row
+ * (for i: for j <= i: zFock(i, j, 1)), then each cell m = 2..numNeighborCells in full, row by row
+ * (for i: for j: zFock(i, j, m)).  Reading restores the upper triangle of R = 0 as the conjugate.
+ * record_bytes is the record length: 16 for recl = 2*dp in bytes (gfortran), 64 for ifort's default
+ * 4-byte record units; the value sits at the start of each record.  zFock is ndim x ndim x
+ * numNeighborCells complex, column-major.  The file name the reference uses is
+ * dataFock/Fock-nspin1 followed by forge_host_parameters_string. */
+int forge_host_write_fock(const forge_setup* s, const double* zFock, const char* path, int64_t record_bytes);
+int forge_host_read_fock(const forge_setup* s, double* zFock, const char* path, int64_t record_bytes);
+
 /* The parameter string of Main.f90:180-183 used in output file names. */
 int forge_host_parameters_string(const forge_setup* s, const char* statename, char* buf, int64_t buflen);
 

@@ -91,3 +91,44 @@ def test_plot_bands_matches_oracle(lib, tmp_path, numk):
     ref = fo.plot_bands_lines(so, go, bands, 0.25)
     assert len(rows) == len(ref)
     assert np.max(np.abs(np.array(rows) - np.round(np.array(ref), 8))) <= 1e-8
+
+
+def _fock_records_reference_order(P, record_bytes):
+    """The record stream of Main.f90:647-672, written with plain numpy loops in the Fortran order."""
+    N, _, NC = P.shape
+    out = bytearray()
+    pad = b"\0" * (record_bytes - 16)
+    for i in range(N):
+        for j in range(i + 1):
+            out += np.complex128(P[i, j, 0]).tobytes() + pad
+    for m in range(1, NC):
+        for i in range(N):
+            for j in range(N):
+                out += np.complex128(P[i, j, m]).tobytes() + pad
+    return bytes(out)
+
+
+@pytest.mark.parametrize("record_bytes", [16, 64])
+def test_fock_checkpoint_format_round_trip(tmp_path, record_bytes):
+    """Fock dump / read (Main.f90:647-672, 202-234): byte-identical to the reference's record order
+    (gfortran and ifort record lengths), and the read restores the conjugate upper triangle of R = 0."""
+    import forge_gb300 as fg
+    S = fg.Setup(ntheta=2, numk=1)
+    N = S.to_struct().ndim
+    rng = np.random.default_rng(7)
+    P = (rng.standard_normal((N, N, 4)) + 1j * rng.standard_normal((N, N, 4))).astype(np.complex128)
+    P[:, :, 0] = (P[:, :, 0] + P[:, :, 0].conj().T) / 2          # P(R=0) Hermitian
+    P = np.asfortranarray(P)
+    path = str(tmp_path / f"Fock-nspin1{fg.parameters_string(S)}")
+    fg.write_fock(S, P, path, record_bytes)
+    data = open(path, "rb").read()
+    assert len(data) == (N * (N + 1) // 2 + 3 * N * N) * record_bytes
+    assert data == _fock_records_reference_order(P, record_bytes)
+    Q = fg.read_fock(S, path, record_bytes)
+    assert np.array_equal(Q, P)
+
+
+def test_fock_checkpoint_rejects_missing_file(tmp_path):
+    import forge_gb300 as fg
+    with pytest.raises(fg.ForgeError):
+        fg.read_fock(fg.Setup(ntheta=2, numk=1), str(tmp_path / "missing"), 16)
