@@ -396,7 +396,9 @@ def main():
                 "warmup": args.warmup, "ms_per_step": cs["t_iter"] * 1e3, "higher_is_better": False,
                 "impl": "reference", "dtype": "f64", "data": "synthetic",
                 "config": {"workload": cfg["name"], "iters": iters, "cpu_parts_s": cs["parts"],
-                           "iterations_source": "recorded plain FP64 run (profiles/scf_records.json)" if rec_plain
+                           "iterations_source": (("ESTIMATED" if rec_plain.get("estimated") else "recorded")
+                                                 + f" plain FP64 iteration count with the {args.mixer} mixer "
+                                                 "(profiles/scf_records.json)") if rec_plain
                            else "itmax (no recorded plain run)"},
                 "cpu_baseline": {"value": val, "unit": "s", "cores": cs["cores"], "kind": "port",
                                  "sample": cs["sample"]},
@@ -471,10 +473,11 @@ def main():
             # the CPU reference runs the plain SCF: the plain iteration count of the record
             rec_plain = _scf_record(cfg["name"], "plain", args.degfactor, args.mixer)
             n_plain = int(rec_plain["n_fp64"]) if rec_plain else iters
+            est = " (estimated count)" if rec_plain and rec_plain.get("estimated") else ""
             line["cpu_baseline"] = {"value": cs["t_iter"] * n_plain, "unit": "s", "cores": cs["cores"],
                                     "kind": "port", "iterations": n_plain,
                                     "sample": cs["sample"] + f"; time-to-SCF = per-iteration time x {n_plain} "
-                                              "plain-SCF iterations"}
+                                              f"plain-SCF iterations{est}"}
     print(json.dumps(line))
 
 

@@ -93,6 +93,8 @@ SIGNATURES = {
     "forge_gpu_scf_iteration": [_P, _P, _P],
     "forge_gpu_set_precision": [_P, _I],
     "forge_gpu_set_mixing": [_P, _I, _I, C.c_double],
+    "forge_gpu_set_refinement": [_P, _I],
+    "forge_selftest_rr_small": [_I, _P, _P, _P, _P],
     "forge_gpu_get_setup": [_P, _P],
     "forge_gpu_synchronize": [_P],
     "forge_gpu_profile": [_P, _I],
@@ -313,6 +315,10 @@ class HartreeFock:
 
     def set_precision(self, precision: str):
         _check(self.lib.forge_gpu_set_precision(self.ctx, FORGE_PREC_MIXED if precision == "mixed" else FORGE_PREC_FP64))
+
+    def set_refinement(self, width: int = 32):
+        """FP64 Rayleigh-Ritz refinement of the top `width` bands after each mixed solve (0: off)."""
+        _check(self.lib.forge_gpu_set_refinement(self.ctx, width))
 
     def set_mixing(self, mode: str = "oda", depth: int = 6, beta: float = 0.7):
         """SCF mixing: "oda" (the reference's OptimalStep) or "pulay" (Anderson / Pulay, `depth` steps)."""

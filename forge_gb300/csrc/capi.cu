@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -71,9 +72,12 @@ int scf_diis_residual(Context& c, const double* y, const double* din, const doub
 int scf_diis_dens(Context& c, const double2* P, double* dens, double* work, ScfScalars* sc);
 int scf_diis_commit(Context& c, ScfScalars* sc);
 size_t scf_diis_parts();
-// mixed-precision eigen-solver (eig_mixed.cu)
+// mixed-precision eigen-solver (eig_mixed.cu) and its FP64 window refinement (rr_window.cu)
 int eig_mixed(cudaStream_t st, EigArgs& g, void* mixed_ws);
 size_t eig_mixed_workspace_bytes(int64_t n, int64_t iu, int64_t batch);
+int rr_window(cudaStream_t st, const double2* H, int64_t strideH, double2* X, int64_t ldx, int64_t strideX, double* w,
+              int64_t iu, int64_t n, int64_t c0, int64_t nw, int64_t batch, void* ws);
+size_t rr_window_workspace_bytes(int64_t n, int64_t batch);
 
 }  // namespace forge
 
@@ -88,6 +92,9 @@ struct forge_ctx {
     DevBuf eigws, mixws; // eigen-solver workspaces
     DevBuf states, sorted_e, sorted_idx, sc, work, y, dens_new, w;
     DevBuf projws, tcerr;  // tensor-core projector staging and its error flag
+    DevBuf rrws;           // FP64 window refinement of the mixed path
+    DevBuf pstates;        // partially occupied states of the fused projector
+    int64_t rr_width = 32; // bands refined in FP64 after each mixed solve (0: off)
     int64_t eig_batch = 0;
     int64_t k_begin = 0, k_end = 0;  // local k range (k_end = 0: all k)
     // mixing: FORGE_MIX_ODA (OptimalStep, the reference) or FORGE_MIX_PULAY (Anderson / Pulay)
@@ -188,7 +195,21 @@ int eig_batch_run(forge_ctx* x, int64_t k0, int64_t nb, int* info) {
     g.ortol_rel = 1e-7;
     eig_bind_workspace(g, x->eigws.ptr);
     if (c.precision == FORGE_PREC_MIXED) {
-        FORGE_TRY(eig_mixed(c.stream, g, x->mixws.ptr));
+        int rc = eig_mixed(c.stream, g, x->mixws.ptr);
+        if (rc == FORGE_ERR_TIMEOUT) {
+            // a bounded tensor-core wait gave up (the kernel drained and freed its TMEM): the
+            // input H(k) is untouched, so the batch is solved again once
+            std::fprintf(stderr, "forge: %s; solving the batch again\n", forge_gpu_last_error());
+            rc = eig_mixed(c.stream, g, x->mixws.ptr);
+        }
+        FORGE_TRY(rc);
+        if (x->rr_width > 0) {
+            // FP64 Rayleigh-Ritz on the top rr_width computed bands (the window around the Fermi level)
+            const int64_t nw = std::min<int64_t>(x->rr_width, iu);
+            FORGE_TRY(x->rrws.ensure(rr_window_workspace_bytes(N, nb)));
+            FORGE_TRY(rr_window(c.stream, g.A, g.strideA, g.X, g.ldx, g.strideX, g.w, iu, N, iu - nw, nw, nb,
+                                x->rrws.ptr));
+        }
     } else {
         FORGE_TRY(eig_fp64(c.stream, g));
     }
@@ -247,7 +268,20 @@ int solve_device(forge_ctx* x, int* info, bool with_projector = true) {
 // P_new = (sum over k of the projector onto bands 1..nLower-1 plus the fully occupied window bands
 // of k, plus the partially occupied states with weight zdeg) / Nk: the sum Main.f90:506-511
 // forms as GetFock + zFockBulk, with the weight-1 window states folded into each k's product.
+int project_fused_once(forge_ctx* x);
+
+// P_new from the solved bands; a bounded tensor-core wait that gave up (FORGE_ERR_TIMEOUT) leaves
+// the eigenvectors untouched, and P_new is formed again once
 int project_fused(forge_ctx* x) {
+    int rc = project_fused_once(x);
+    if (rc == FORGE_ERR_TIMEOUT) {
+        std::fprintf(stderr, "forge: %s; forming P_new again\n", forge_gpu_last_error());
+        rc = project_fused_once(x);
+    }
+    return rc;
+}
+
+int project_fused_once(forge_ctx* x) {
     Context& c = x->c;
     const int64_t N = c.N, Nk = c.Nk;
     const size_t NN = (size_t)N * N;
@@ -272,9 +306,12 @@ int project_fused(forge_ctx* x) {
     for (int64_t q = nocc - npart; q < nocc; ++q)
         if (st[q].k >= kb && st[q].k < ke) part.push_back(st[q]);
     if (!part.empty()) {
-        FORGE_CUDA(cudaMemcpyAsync(x->states.ptr, part.data(), part.size() * sizeof(WinState), cudaMemcpyHostToDevice,
-                                   c.stream));
-        FORGE_TRY(window_projector_fp64(c.stream, x->states.as<WinState>(), (int64_t)part.size(), c.X.as<double2>(),
+        // the partial states go to their own buffer: x->states keeps the sorted list (a second
+        // formation of P_new reads it again)
+        FORGE_TRY(x->pstates.ensure(part.size() * sizeof(WinState)));
+        FORGE_CUDA(cudaMemcpyAsync(x->pstates.ptr, part.data(), part.size() * sizeof(WinState),
+                                   cudaMemcpyHostToDevice, c.stream));
+        FORGE_TRY(window_projector_fp64(c.stream, x->pstates.as<WinState>(), (int64_t)part.size(), c.X.as<double2>(),
                                         c.N, c.N * c.nUpper, c.N, x->Pn.as<double2>()));
     }
     FORGE_CUDA(cudaMemsetAsync(c.bulk.ptr, 0, 4 * NN * sizeof(double2), c.stream));
@@ -614,7 +651,7 @@ int forge_gpu_finalize(forge_ctx* x) {
                       &c.dens_in, &c.V_old, &c.H, &c.X, &c.bands, &c.evals, &c.kvecs, &c.kphase, &c.bphase,
                       &c.sort_idx, &c.sort_e, &c.red, &c.scalars, &x->te, &x->Pn, &x->win, &x->eigws, &x->mixws,
                       &x->states, &x->sorted_e, &x->sorted_idx, &x->sc, &x->work, &x->y, &x->dens_new, &x->w,
-                      &x->projws, &x->tcerr};
+                      &x->projws, &x->tcerr, &x->diis_hist, &x->diis_rprev, &x->diis_part, &x->rrws, &x->pstates};
     for (DevBuf* b : bufs) b->release();
     if (c.stream) cudaStreamDestroy(c.stream);
     delete x;
@@ -632,6 +669,16 @@ int forge_gpu_set_precision(forge_ctx* x, int64_t precision) {
         x->eig_batch = 0;
         diis_reset(x);   // the residual map changes with the precision
     }
+    return 0;
+}
+
+int forge_gpu_set_refinement(forge_ctx* x, int64_t width) {
+    FORGE_TRY(check_ctx(x));
+    if (width < 0 || width > 32) {
+        set_error(FORGE_ERR_ARG, "set_refinement: width %lld outside 0..32", (long long)width);
+        return FORGE_ERR_ARG;
+    }
+    x->rr_width = width;
     return 0;
 }
 
@@ -807,6 +854,14 @@ int forge_gpu_zheevr_batch(forge_ctx* x, int64_t nb, const double* A, int64_t iu
     g.ortol_rel = 1e-7;
     eig_bind_workspace(g, ws.ptr);
     rc = (c.precision == FORGE_PREC_MIXED) ? eig_mixed(c.stream, g, mws.ptr) : eig_fp64(c.stream, g);
+    DevBuf rws;
+    if (!rc && c.precision == FORGE_PREC_MIXED && x->rr_width > 0) {
+        // the same FP64 window refinement as the SCF's solves
+        const int64_t nw = std::min<int64_t>(x->rr_width, iu);
+        rc = rws.ensure(rr_window_workspace_bytes(N, nb));
+        if (!rc)
+            rc = rr_window(c.stream, g.A, g.strideA, g.X, g.ldx, g.strideX, g.w, iu, N, iu - nw, nw, nb, rws.ptr);
+    }
     std::vector<int> fails(nb);
     if (!rc) {
         FORGE_CUDA(cudaMemcpyAsync(w, dw.ptr, nb * iu * sizeof(double), cudaMemcpyDeviceToHost, c.stream));

@@ -200,6 +200,12 @@ int forge_gpu_scf_iteration(forge_ctx* ctx, double* Energies, forge_iter_report*
  * (P_in, P_new) and Step is 1. */
 int forge_gpu_set_mixing(forge_ctx* ctx, int64_t mode, int64_t depth, double beta);
 
+/* FP64 Rayleigh-Ritz refinement after every FORGE_PREC_MIXED eigen-solve (no counterpart in the
+ * reference): the top `width` computed eigenvectors of each k (the zdiagRed window and the bands
+ * below it, width 0..32, default 32, 0 = off) are re-solved in their span with FP64 products
+ * against the FP64 H(k): Y = H X, G = X^H Y, S = X^H X, then G z = theta S z on the host. */
+int forge_gpu_set_refinement(forge_ctx* ctx, int64_t width);
+
 /* Selects FORGE_PREC_FP64 or FORGE_PREC_MIXED for subsequent solves. */
 int forge_gpu_set_precision(forge_ctx* ctx, int64_t precision);
 
@@ -224,6 +230,12 @@ int forge_gpu_profile_read(forge_ctx* ctx, double* ms, int64_t* launches, double
  * all row-major fp32 host arrays.  Used by the tests to validate the tensor-core GEMM. */
 int forge_gpu_selftest_tc_gemm(int64_t M, int64_t N, int64_t K, int64_t batch, const float* A, const float* B,
                                float* D);
+
+/* Diagnostic, host only: the small dense step of the window refinement.  G, S: n x n Hermitian
+ * (complex, column-major, interleaved re/im doubles), n <= 32.  Returns theta (ascending) and
+ * M = L^{-H} U, with S = L L^H and L^{-1} G L^{-H} = U diag(theta) U^H, so that G M = S M diag(theta)
+ * and M^H S M = I.  Returns 1 if S is not positive definite. */
+int forge_selftest_rr_small(int64_t n, const double* G, const double* S, double* theta, double* M);
 
 /* Learned SCF warm start (no counterpart in the reference, which starts from the non-interacting
  * guess or a checkpoint): an MLP din -> 128 -> 128 -> 128 -> dout (SiLU), BF16 weights, FP32

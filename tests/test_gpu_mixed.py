@@ -60,3 +60,33 @@ def test_mixed_zheevr_model_hamiltonian(lib):
         X = Z[:, :, b]
         assert np.max(np.abs(X.conj().T @ X - np.eye(iu))) <= 1e-4
     hf.close()
+
+
+def test_fp64_window_refinement_recovers_fp64_accuracy(lib):
+    """The FP64 Rayleigh-Ritz step after the mixed solve (forge_gpu_set_refinement): the refined top
+    32 eigenpairs reach FP64-level eigenvalues and orthonormality, the unrefined ones stay FP32-level."""
+    hf = _hf(5)
+    N = hf.N
+    rng = np.random.default_rng(21)
+    A = rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))
+    M = (A + A.conj().T) / 2
+    iu = N // 2 + 10
+    wo, Zo = fo.eigh_lower(M, iu)
+    scale = np.max(np.abs(np.linalg.eigvalsh(M)))
+    hf.set_refinement(0)
+    w0, Z0, info0 = hf.zheevr_batch(np.tril(M)[:, :, None], iu)
+    hf.set_refinement(32)
+    w1, Z1, info1 = hf.zheevr_batch(np.tril(M)[:, :, None], iu)
+    assert info0 == 0 and info1 == 0
+    win = slice(iu - 32, iu)
+    err0 = np.max(np.abs(w0[win, 0] - wo[win]))
+    err1 = np.max(np.abs(w1[win, 0] - wo[win]))
+    assert err0 >= 1e-9 * scale                  # the mixed solve alone is FP32-accurate
+    # Ritz values of an FP32-accurate subspace: errors of second order in the subspace angle
+    assert err1 <= 1e-9 * scale
+    X = Z1[:, win, 0]
+    assert np.max(np.abs(X.conj().T @ X - np.eye(32))) <= 1e-12
+    assert np.max(np.abs(M @ X - X * w1[win, 0])) <= 2e-5 * scale * np.sqrt(N)
+    # the bands below the window are untouched
+    assert np.array_equal(Z1[:, :iu - 32, 0], Z0[:, :iu - 32, 0])
+    hf.close()

@@ -132,3 +132,33 @@ def test_fock_checkpoint_rejects_missing_file(tmp_path):
     import forge_gb300 as fg
     with pytest.raises(fg.ForgeError):
         fg.read_fock(fg.Setup(ntheta=2, numk=1), str(tmp_path / "missing"), 16)
+
+
+@pytest.mark.parametrize("n,seed", [(1, 0), (5, 1), (32, 2)])
+def test_rayleigh_ritz_small_solve_matches_numpy(n, seed):
+    """The nw x nw step of the mixed path's FP64 window refinement (forge_selftest_rr_small, host
+    code): the generalised eigenvalues of (G, S) match numpy, G M = S M theta and M^H S M = I."""
+    import ctypes as C
+    import forge_gb300 as fg
+    lib = fg.load_library()
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((200, n)) + 1j * rng.standard_normal((200, n))
+    X /= np.linalg.norm(X, axis=0)
+    X += 1e-7 * (rng.standard_normal(X.shape) + 1j * rng.standard_normal(X.shape))   # nearly orthonormal
+    H = rng.standard_normal((200, 200)) + 1j * rng.standard_normal((200, 200))
+    H = (H + H.conj().T) / 2
+    G = np.asfortranarray(X.conj().T @ H @ X)
+    S = np.asfortranarray(X.conj().T @ X)
+    th = np.zeros(n)
+    M = np.zeros((n, n), dtype=np.complex128, order="F")
+    rc = lib.forge_selftest_rr_small(n, G.ctypes.data_as(C.c_void_p), S.ctypes.data_as(C.c_void_p),
+                                     th.ctypes.data_as(C.c_void_p), M.ctypes.data_as(C.c_void_p))
+    assert rc == 0
+    Ls = np.linalg.cholesky(S)
+    Li = np.linalg.inv(Ls)
+    ref = np.linalg.eigvalsh(Li @ G @ Li.conj().T)
+    scale = max(1.0, np.max(np.abs(ref)))
+    assert np.max(np.abs(th - ref)) <= 1e-12 * scale
+    assert np.all(np.diff(th) >= 0)
+    assert np.max(np.abs(G @ M - S @ M * th)) <= 1e-11 * scale
+    assert np.max(np.abs(M.conj().T @ S @ M - np.eye(n))) <= 1e-12
