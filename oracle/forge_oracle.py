@@ -870,10 +870,57 @@ def plain_guess(s: Setup, g: Geometry, T: PairTables):
     return P, dict(sol=sol, EF=EF, nocc=nocc, npart=npart, degf=degf)
 
 
+class PulayMixer:
+    """Anderson / Pulay mixing of the density matrix, the library's FORGE_MIX_PULAY option (no
+    counterpart in the reference, which mixes with OptimalStep only).
+
+    x_next = x + beta r - sum_i g_i (dX_i + beta dR_i), r = P_new - P_in, g minimising
+    |r - sum_i g_i dR_i|, over the last `depth` difference pairs.  The pairs and the previous
+    residual are stored in complex64, as on the device; x and r stay complex128.
+    """
+
+    def __init__(self, depth: int = 6, beta: float = 0.7):
+        self.depth, self.beta = depth, beta
+        self.pairs = []          # [dX (c64), dR (c64)], oldest first
+        self.pending = None      # dX of the last step, waiting for its dR
+        self.rprev = None
+
+    def step(self, P_in, P_new):
+        r = P_new - P_in
+        if self.rprev is None:
+            x = P_in + self.beta * r
+        else:
+            dR = (r - self.rprev.astype(np.complex128)).astype(np.complex64)
+            self.pairs.append([self.pending, dR])
+            if len(self.pairs) > self.depth:
+                self.pairs.pop(0)
+            k = len(self.pairs)
+            G = np.zeros((k, k))
+            b = np.zeros(k)
+            for i, (_, di) in enumerate(self.pairs):
+                d64 = di.astype(np.complex128)
+                b[i] = float(np.real(np.vdot(d64, r)))
+                for j, (_, dj) in enumerate(self.pairs):
+                    G[i, j] = float(np.real(np.vdot(d64, dj.astype(np.complex128))))
+            G[np.diag_indices(k)] += 1e-10 * np.max(np.diag(G))
+            try:
+                gam = np.linalg.solve(G, b)
+            except np.linalg.LinAlgError:
+                gam = np.zeros(k)
+            x = P_in + self.beta * r
+            for gi, (dx, dr) in zip(gam, self.pairs):
+                x = x - gi * (dx.astype(np.complex128) + self.beta * dr.astype(np.complex128))
+        self.pending = (x - P_in).astype(np.complex64)
+        self.rprev = r.astype(np.complex64)
+        return x
+
+
 def run_scf(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTables] = None, LR=None,
             P_init=None, itmax: Optional[int] = None, residual_tol: Optional[float] = None,
-            keep_history: bool = False):
-    """Main.f90:236-679 for numS=1: initial guess, energies, potential, then the SCF loop with ODA mixing.
+            keep_history: bool = False, mixer: Optional[PulayMixer] = None):
+    """Main.f90:236-679 for numS=1: initial guess, energies, potential, then the SCF loop with ODA mixing
+    (or, with ``mixer``, Anderson / Pulay mixing: the state is the mixer's output, Step is 1 and the
+    residual is that of (P_in, P_new)).
 
     Stops after ``itmax`` iterations (reference behaviour) or earlier when
     ``residual_tol`` is given and the mean-field residual drops below it.
@@ -908,14 +955,24 @@ def run_scf(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTables] = No
         P_new = (Pw + sol["bulk"]) / complex(float(s.Nk), 0.0)
         E_in, Etot_in = E, Etot
         dens_new = np.real(np.diagonal(P_new[0])).copy()
-        step, E, t1, t2 = optimal_step(s, T, LR, P_new, P_in, dens_new, dens_in, E_in)
-        Etot = E.total(s)
-        P = step * P_new + (1.0 - step) * P_in
-        dens = np.real(np.diagonal(P[0])).copy()
-        dn = float(np.max(np.abs(dens - dens_in)))
-        V_old = V
-        V = potential(s, LR, dens)
-        res = hf_residual(s, T, V, V_old, P, P_in)
+        if mixer is not None:
+            res = hf_residual(s, T, potential(s, LR, dens_new), V, P_new, P_in)
+            P = mixer.step(P_in, P_new)
+            step, t1, t2 = 1.0, float("nan"), float("nan")
+            dens = np.real(np.diagonal(P[0])).copy()
+            E = energies(s, T, LR, P, dens)
+            Etot = E.total(s)
+            dn = float(np.max(np.abs(dens - dens_in)))
+            V = potential(s, LR, dens)
+        else:
+            step, E, t1, t2 = optimal_step(s, T, LR, P_new, P_in, dens_new, dens_in, E_in)
+            Etot = E.total(s)
+            P = step * P_new + (1.0 - step) * P_in
+            dens = np.real(np.diagonal(P[0])).copy()
+            dn = float(np.max(np.abs(dens - dens_in)))
+            V_old = V
+            V = potential(s, LR, dens)
+            res = hf_residual(s, T, V, V_old, P, P_in)
         dens_in = dens.copy()
         P_in = P.copy()
         logs.append(IterationLog(it, dn, step, Etot_in - Etot, Etot_in, E_in.kinetic, E_in.fock,

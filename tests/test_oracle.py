@@ -146,3 +146,18 @@ def test_golden_fixtures_reproduce():
     assert np.max(np.abs(r["P"] - gd["P"])) < 1e-10
     assert np.max(np.abs(np.array([l.E_in for l in r["logs"]]) - gd["E_in"])) < 1e-9
     assert np.max(np.abs(r["LR"] - gd["LR"])) < 1e-13
+
+
+def test_oracle_pulay_mixing_reaches_the_optimalstep_fixed_point():
+    """The oracle's Anderson / Pulay mixer (the library's FORGE_MIX_PULAY restated) converges to the
+    fixed point the reference's OptimalStep SCF reaches, in fewer iterations."""
+    so = fo.Setup(ntheta=2, numk=3, nfilling=2.0)
+    g = fo.build_geometry(so)
+    T = fo.pair_tables(so, g)
+    LR = fo.long_range_interaction(so, g)
+    oda = fo.run_scf(so, g, T, LR, itmax=400, residual_tol=1e-11)
+    pul = fo.run_scf(so, g, T, LR, itmax=400, residual_tol=1e-11, mixer=fo.PulayMixer(6, 0.7))
+    assert oda["logs"][-1].residual < 1e-11 and pul["logs"][-1].residual < 1e-11
+    assert len(pul["logs"]) < len(oda["logs"])
+    assert np.max(np.abs(pul["P"] - oda["P"])) <= 1e-9
+    assert abs(pul["Etot"] - oda["Etot"]) / so.ndim <= 1e-9
