@@ -1,17 +1,24 @@
 """Benchmark: time-to-SCF of FORGE's real-space Hartree-Fock loop on one GB300.
 
-One step = one SCF iteration of the hot path (H(k) assembly for all k, batched
-eigen-solve of eigenpairs 1..N/2+10, density-matrix projectors, sort / Fermi level,
-ODA line search, mixing and Hartree potential) with every array resident in HBM.
-The SCF is run from its starting guess: W warm-up iterations (untimed), K timed
-iterations (CUDA events on the library's stream), then untimed iterations until the
-mean-field residual drops below the tolerance, which gives the iteration count.
-value = time-to-SCF = mean timed iteration time x iterations to reach the residual.
+One step = one SCF iteration of the hot path (H(k) assembly for all k, batched eigen-solve of
+eigenpairs 1..N/2+10, density-matrix projectors, sort / Fermi level, energies, mixing and Hartree
+potential) with every array resident in HBM, timed with CUDA events on the library's stream.
 
-Workloads (BASELINE configs): 4 = 1.05 deg twisted bilayer, m=31, N=11908, 4x4 k, nu=+2,
-eps=10 (headline, default); 1 = m=10, N=1324, 12x12 k, nu=+2; 2 = m=20, N=5044, 8x8 k,
-nu=-2, eps=8; 0 = m=5, N=364, 6x6 k, nu=0.  Inputs are synthetic by construction (the
-geometry and the model are generated from the parameters); nothing is read from disk.
+value = time-to-SCF: the starting guess, then the SCF iterations until the mean-field residual is
+below --tol (1e-6 eV).  W warm-up iterations are charged at the timed mean of their precision; the K
+timed iterations and every later one at their own event time.  With --converge the run continues
+to the tolerance; otherwise the iteration counts (and, if this run did none, the FP64 iteration
+time) come from the recorded --converge run of the same workload, mode, DegFactor rule and mixer in
+profiles/scf_records.json, and config.iterations_source says so.
+
+Modes: fast = learned warm start + mixed-precision iterations + FP64 finish; mixed = plain guess +
+mixed + FP64 finish; plain = plain guess + FP64.  Mixers: Anderson/Pulay (depth 6, default) or the
+reference's OptimalStep.
+
+Workloads: 4 = 1.05 deg twisted bilayer, m=31, N=11908, 4x4 k, nu=+2, eps=10 (headline, default);
+1 = m=10, N=1324, 12x12 k, nu=+2; 2 = m=20, N=5044, 8x8 k, nu=-2, eps=8; 0 = m=5, N=364, 6x6 k,
+nu=0.  Inputs are synthetic by construction (the geometry and the model are generated from the
+parameters); nothing is read from disk.
 """
 from __future__ import annotations
 
@@ -355,8 +362,7 @@ def main():
                     help="fast: learned warm start + mixed-precision iterations; mixed: plain guess + mixed; "
                          "plain: plain guess + FP64")
     ap.add_argument("--mixer", default="pulay", choices=["pulay", "oda"],
-                    help="SCF mixing of both modes: Anderson/Pulay (the benchmark description's depth-6 Pulay) or the "
-                         "reference's OptimalStep")
+                    help="SCF mixing of both modes: Anderson/Pulay or the reference's OptimalStep")
     ap.add_argument("--mix-depth", type=int, default=6)
     ap.add_argument("--mix-beta", type=float, default=0.7)
     ap.add_argument("--degfactor", default="corrected", choices=["corrected", "reference"],

@@ -1,6 +1,6 @@
 """Trains the warm-start networks on converged fields that the SCF itself produces.
 
-Training systems follow the uneven-size set of the benchmark description: twisted bilayers
+Training systems are an uneven-size set: twisted bilayers
 (m, m+1) for m = 8, 12, 16, and the alternating-twist trilayer at m = 12, at several fillings
 and dielectric constants.  Each is converged with the mixed-precision SCF to a mean-field
 residual of 1e-5 eV (training targets need no more), then site and bond samples are drawn and

@@ -191,7 +191,7 @@ int forge_gpu_prepare_state(forge_ctx* ctx, double* Energies);
 int forge_gpu_scf_iteration(forge_ctx* ctx, double* Energies, forge_iter_report* report);
 
 /* Mixing of forge_gpu_scf_iteration (no counterpart in the reference, which mixes with OptimalStep
- * only; the Anderson / Pulay option follows the benchmark description's "Pulay mixing depth 6"):
+ * only):
  * FORGE_MIX_ODA (default) or FORGE_MIX_PULAY with `depth` (1..7) previous steps and mixing weight
  * beta (0..1]: P_in <- P_in + beta r - sum_i g_i (dP_i + beta dr_i), r = P_new - P_in, with g
  * minimising |r - sum_i g_i dr_i|.  The history (complex64 differences, 2 x 4 N^2 x 8 bytes per
