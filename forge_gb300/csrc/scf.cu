@@ -386,6 +386,7 @@ __global__ void k_oda(ScfScalars* sc, EnergyParams p, int mode) {
     energies_at(sc, 1.0, E1);
     if (mode == 1) {
         for (int t = 0; t < 4; ++t) sc->Eout[t] = E1[t];
+        sc->Etot_in = total_energy(p, sc->Ein);
         sc->Etot_out = total_energy(p, E1);
         sc->step = 1.0;
         return;
