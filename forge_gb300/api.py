@@ -117,6 +117,8 @@ SIGNATURES = {
     "forge_host_plot_bands": [_P, _P, _D, _P, _P, _P, C.c_char_p],
     "forge_host_write_fock": [_P, _P, C.c_char_p, _I],
     "forge_host_read_fock": [_P, _P, C.c_char_p, _I],
+    "forge_host_sort_energies_2spins": [_I, _I, _P, _P, _P],
+    "forge_host_fermi_2spins": [_P, _P, _P, _P, _P, _P, _P, _P],
 }
 
 _LIB = None
@@ -261,6 +263,36 @@ def read_fock(setup: Setup, path: str, record_bytes: int = 16) -> np.ndarray:
     P = np.zeros((s.ndim, s.ndim, s.numNeighborCells), dtype=np.complex128, order="F")
     _check(load_library().forge_host_read_fock(C.byref(s), _ptr(P), path.encode(), record_bytes))
     return P
+
+
+def sort_energies_2spins(numk: int, numb: int, WindowSort_2Spins, SortedEnergies_1Spin) -> np.ndarray:
+    """SortEnergies_2Spins (HartreeFock.f90:929-1004) through forge_host_sort_energies_2spins.
+
+    WindowSort_2Spins is W(i, spin) (2 x 2), SortedEnergies_1Spin the (numb*Nk, 2) per-spin sorted
+    energies; returns SortedEnergies_2Spins (2*numb*Nk, 2): merged energies and spin labels 1.0 / 2.0.
+    """
+    n = numb * numk * numk
+    W = _f(np.asarray(WindowSort_2Spins, dtype=np.int64).reshape(2, 2), np.int64)
+    se = _f(np.asarray(SortedEnergies_1Spin, dtype=np.float64).reshape(n, 2), np.float64)
+    out = np.zeros((2 * n, 2), dtype=np.float64, order="F")
+    _check(load_library().forge_host_sort_energies_2spins(numk, numb, _ptr(W), _ptr(se), _ptr(out)))
+    return out
+
+
+def fermi_2spins(setup: Setup, SortedEnergies_1Spin) -> dict:
+    """Main.f90:416-453 (numS = 2) through forge_host_fermi_2spins: the merged list, nFermiLevel,
+    FermiEnergy, nOccStates(2), nPartOccStates(2) and DegFactor."""
+    s = setup.to_struct()
+    n = s.numb * s.numk * s.numk
+    se = _f(np.asarray(SortedEnergies_1Spin, dtype=np.float64).reshape(n, 2), np.float64)
+    merged = np.zeros((2 * n, 2), dtype=np.float64, order="F")
+    nF, EF, deg = C.c_int64(), C.c_double(), C.c_double()
+    nocc = np.zeros(2, np.int64)
+    npart = np.zeros(2, np.int64)
+    _check(load_library().forge_host_fermi_2spins(C.byref(s), _ptr(se), _ptr(merged), C.byref(nF), C.byref(EF),
+                                                  _ptr(nocc), _ptr(npart), C.byref(deg)))
+    return dict(SortedEnergies_2Spins=merged, nFermiLevel=nF.value, FermiEnergy=EF.value,
+                nOccStates=nocc.tolist(), nPartOccStates=npart.tolist(), DegFactor=deg.value)
 
 
 def parameters_string(setup: Setup, statename: str = "SSS") -> str:

@@ -358,6 +358,96 @@ int forge_host_read_fock(const forge_setup* s, double* zFock, const char* path, 
     return ok ? 0 : FORGE_ERR_ARG;
 }
 
+// SortEnergies_2Spins (HartreeFock.f90:929-1004).  Counters are 1-based as in the reference; the
+// run loops test their bound before reading, where the Fortran reads one element past the list
+// (the comparison result is discarded there, so the merged list is the same).
+int forge_host_sort_energies_2spins(int64_t numk, int64_t numb, const int64_t* W, const double* se,
+                                    double* out) {
+    if (numk < 1 || numb < 1 || !W || !se || !out) return FORGE_ERR_ARG;
+    const int64_t Nk = numk * numk, n = numb * Nk;
+    // W(i, sp) is W[(i-1) + 2*(sp-1)]; every front block and merge bound must lie inside the lists
+    for (int sp = 0; sp < 2; ++sp)
+        if (W[2 * sp] < 1 || W[2 * sp + 1] < W[2 * sp] || W[2 * sp + 1] > numb + 1) return FORGE_ERR_ARG;
+    if (W[2] > 1 && (W[0] - 1) * Nk + 1 > n) return FORGE_ERR_ARG;  // the spin-2 front block reads s2(ncount1)
+    const double* s1 = se - 1;      // SortedEnergies_1Spin(:, 1), 1-based
+    const double* s2 = se + n - 1;  // SortedEnergies_1Spin(:, 2)
+    double* oe = out;
+    double* os = out + 2 * n;
+    int64_t cb = 0, c1 = 1, c2 = 1;
+    auto put = [&](double e, int sp) {
+        oe[cb] = e;
+        os[cb] = (double)sp;
+        ++cb;
+    };
+    for (int64_t q = 0; q < (W[0] - 1) * Nk; ++q) put(s1[c1++], 1);
+    // HartreeFock.f90:949 reads the spin-2 list at the spin-1 counter
+    for (int64_t q = 0; q < (W[2] - 1) * Nk; ++q) {
+        put(s2[c1], 2);
+        ++c2;
+    }
+    const int64_t lim1 = Nk * (W[1] - 1), lim2 = Nk * (W[3] - 1);
+    while (c1 <= lim1 && c2 <= lim2) {
+        if (s1[c1] <= s2[c2]) {
+            put(s1[c1++], 1);
+            while (c1 <= n && s1[c1] <= s2[c2]) put(s1[c1++], 1);
+            put(s2[c2++], 2);
+        } else {
+            put(s2[c2++], 2);
+            while (c2 <= n && s2[c2] <= s1[c1]) put(s2[c2++], 2);
+            put(s1[c1++], 1);
+        }
+    }
+    while (c1 <= n) put(s1[c1++], 1);
+    while (c2 <= n) put(s2[c2++], 2);
+    return cb == 2 * n ? 0 : FORGE_ERR_ARG;
+}
+
+// Main.f90:416-453: window, merge, the common Fermi level and the per-spin occupations.
+int forge_host_fermi_2spins(const forge_setup* s, const double* SortedEnergies_1Spin, double* SortedEnergies_2Spins,
+                            int64_t* nFermiLevel, double* FermiEnergy, int64_t* nOccStates, int64_t* nPartOccStates,
+                            double* DegFactor) {
+    if (!s || !SortedEnergies_1Spin || !nFermiLevel || !FermiEnergy || !nOccStates || !nPartOccStates || !DegFactor)
+        return FORGE_ERR_ARG;
+    const int64_t Nk = s->numk * s->numk, n = s->numb * Nk, NP = s->NeutralityPoint;
+    const int64_t W[4] = {NP - 1, NP + 2 + 1, NP - 1, NP + 2 + 1};  // nWindowSort_2Spins, Main.f90:416-419
+    std::vector<double> own;
+    double* merged = SortedEnergies_2Spins;
+    if (!merged) {
+        own.resize((size_t)(4 * n));
+        merged = own.data();
+    }
+    int rc = forge_host_sort_energies_2spins(s->numk, s->numb, W, SortedEnergies_1Spin, merged);
+    if (rc) return rc;
+    // nFermiLevel = numS * nint(Nk*NP + Nk/2*nfilling), Fortran nint rounding half away from zero
+    const double x = (double)(Nk * NP) + (double)Nk / 2.0 * s->nfilling;
+    const int64_t nF = 2 * (int64_t)(x >= 0 ? std::floor(x + 0.5) : -std::floor(-x + 0.5));
+    if (nF < 1 || nF >= 2 * n) return FORGE_ERR_ARG;
+    const double ef = (merged[nF - 1] + merged[nF]) / 2.0;
+    const double tol = s->EnergyTolerance;
+    int64_t nocc[2] = {0, 0}, npart[2] = {0, 0};
+    for (int64_t q = 0; q < 2 * n; ++q) {
+        const int k = merged[2 * n + q] == 1.0 ? 0 : 1;
+        const double e = merged[q];
+        if ((e - ef) < -tol) {
+            ++nocc[k];
+        } else if (std::fabs(e - ef) < tol) {
+            ++npart[k];
+            ++nocc[k];
+        }
+    }
+    double deg = 0.0;
+    if (npart[0] != 0 || npart[1] != 0)
+        deg = 1.0 / (double)(npart[0] + npart[1]) * (double)(nF + npart[0] + npart[1] - nocc[0] - nocc[1]);
+    *nFermiLevel = nF;
+    *FermiEnergy = ef;
+    nOccStates[0] = nocc[0];
+    nOccStates[1] = nocc[1];
+    nPartOccStates[0] = npart[0];
+    nPartOccStates[1] = npart[1];
+    *DegFactor = deg;
+    return 0;
+}
+
 int forge_host_run_scf(forge_ctx* ctx, const forge_scf_options* opts, const double* zFock_init,
                        forge_scf_result* result, forge_iter_report* reports) {
     if (!ctx || !opts || !result) return FORGE_ERR_ARG;

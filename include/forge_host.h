@@ -58,6 +58,24 @@ typedef struct forge_scf_result {
 int forge_host_run_scf(forge_ctx* ctx, const forge_scf_options* opts, const double* zFock_init,
                        forge_scf_result* result, forge_iter_report* reports);
 
+/* SortEnergies_2Spins (HartreeFock.f90:929-1004), same arguments: WindowSort_2Spins is the 2 x 2
+ * column-major window table W(i, spin), SortedEnergies_1Spin the (numb*Nk) x 2 column-major per-spin
+ * sorted energies (forge_gpu_sort_energies of each spin), SortedEnergies_2Spins the (2*numb*Nk) x 2
+ * output: the merged energies, then the spin label of each (1.0 or 2.0).  The first (W(1,sp)-1)*Nk
+ * states of each spin are copied in front, the states up to Nk*(W(2,sp)-1) are merged, the tails are
+ * appended spin 1 first; as in the reference, the spin-2 front block repeats the spin-2 energy at
+ * position (W(1,1)-1)*Nk+1.  FORGE_ERR_ARG when a window lies outside 1..numb+1. */
+int forge_host_sort_energies_2spins(int64_t numk, int64_t numb, const int64_t* WindowSort_2Spins,
+                                    const double* SortedEnergies_1Spin, double* SortedEnergies_2Spins);
+
+/* Main.f90:416-453 (numS = 2): nWindowSort_2Spins = (NP-1, NP+3) for both spins, the merge above,
+ * nFermiLevel = 2*nint(Nk*NP + Nk/2*nfilling), FermiEnergy between merged states nFermiLevel and
+ * nFermiLevel+1, nOccStates(2) / nPartOccStates(2) counted per spin label, and DegFactor over both
+ * spins (0 when no state is partially occupied).  SortedEnergies_2Spins may be NULL. */
+int forge_host_fermi_2spins(const forge_setup* s, const double* SortedEnergies_1Spin, double* SortedEnergies_2Spins,
+                            int64_t* nFermiLevel, double* FermiEnergy, int64_t* nOccStates, int64_t* nPartOccStates,
+                            double* DegFactor);
+
 /* PlotBands (TightBinding.f90:275-369): writes Bands(numb, Nk) - FermiEnergy along the
  * K - Gamma - M - K path of k-grid points to the file `path` (the reference's unit 99). */
 int forge_host_plot_bands(const forge_setup* s, const double* Bands, double FermiEnergy,

@@ -692,10 +692,14 @@ def fortran_nint(x: float) -> int:
     return int(math.floor(x + 0.5)) if x >= 0 else -int(math.floor(-x + 0.5))
 
 
-def fermi_level(s: Setup, sorted_e):
-    """Main.f90:400-412: nFermiLevel, FermiEnergy, nOccStates, nPartOccStates, DegFactor."""
+def fermi_level(s: Setup, sorted_e, spin_factor: Optional[int] = None):
+    """Main.f90:400-412: nFermiLevel, FermiEnergy, nOccStates, nPartOccStates, DegFactor.
+
+    ``spin_factor`` replaces the numS factor of nFermiLevel; the initial guess (Main.f90:255) has none.
+    """
     Nk = s.Nk
-    nF = s.numS * fortran_nint(float(Nk * s.NeutralityPoint) + float(Nk) / 2.0 * s.nfilling)
+    fac = s.numS if spin_factor is None else spin_factor
+    nF = fac * fortran_nint(float(Nk * s.NeutralityPoint) + float(Nk) / 2.0 * s.nfilling)
     EF = (sorted_e[nF - 1] + sorted_e[nF]) / 2.0
     tol = s.EnergyTolerance
     nocc = 0
@@ -793,12 +797,17 @@ def energies(s: Setup, T: PairTables, LR, P, dens) -> Energies:
     return Energies(kinetic_energy(s, T, P), fock_energy(s, T, P), eh, eu)
 
 
-def optimal_step(s: Setup, T: PairTables, LR, P_new, P_in, dens, dens_in, E_in: Energies):
-    """OptimalStep (HartreeFock.f90:1148-1227): returns (Step, energies at Step, E1, E_half)."""
+def optimal_step(s: Setup, T: PairTables, LR, P_new, P_in, dens, dens_in, E_in: Energies, energy_fn=None):
+    """OptimalStep (HartreeFock.f90:1148-1227): returns (Step, energies at Step, E1, E_half).
+
+    ``energy_fn`` is ``energies`` (numS=1, the default) or ``energies_2spins`` (numS=2, spin-stacked
+    P and densities); the step rule is the same for both.
+    """
+    energies_ = energies if energy_fn is None else energy_fn
     c0 = E_in.total(s)
-    E1 = energies(s, T, LR, P_new, dens)
+    E1 = energies_(s, T, LR, P_new, dens)
     t1 = E1.total(s)
-    Eh = energies(s, T, LR, 0.5 * (P_in + P_new), .5 * (dens + dens_in))
+    Eh = energies_(s, T, LR, 0.5 * (P_in + P_new), .5 * (dens + dens_in))
     t2 = Eh.total(s)
     c1 = 4.0 * t2 - t1 - 3.0 * c0
     c2 = t1 - c0 - c1
@@ -808,7 +817,7 @@ def optimal_step(s: Setup, T: PairTables, LR, P_new, P_in, dens, dens_in, E_in: 
         step = 1.0
     else:
         step = s.StepAlternative
-    Es = energies(s, T, LR, (1.0 - step) * P_in + step * P_new, (1 - step) * dens_in + step * dens)
+    Es = energies_(s, T, LR, (1.0 - step) * P_in + step * P_new, (1 - step) * dens_in + step * dens)
     return step, Es, t1, t2
 
 
@@ -864,7 +873,7 @@ def plain_guess(s: Setup, g: Geometry, T: PairTables):
     V0 = np.zeros(N)
     sol = solve(s, g, T, V0, P0)
     se, _, moms, sv, _, _ = sort_energies_1spin(s, g, sol["bands"], sol["evecs"])
-    nF, EF, nocc, npart, degf = fermi_level(s, se)
+    nF, EF, nocc, npart, degf = fermi_level(s, se, spin_factor=1)
     P = get_fock(s, g, sv, moms, nocc, npart, degf)
     P = (P + sol["bulk"]) / complex(float(s.Nk), 0.0)
     return P, dict(sol=sol, EF=EF, nocc=nocc, npart=npart, degf=degf)
@@ -979,6 +988,201 @@ def run_scf(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTables] = No
                                  E_in.hartree, E_in.hubbard, EF, nocc, npart, res))
         last = dict(bands=sol["bands"], eigs=sol["eigs"], EF=EF, nocc=nocc, npart=npart, degf=degf,
                     P_new=P_new, step=step, E1=t1, Ehalf=t2)
+        if keep_history:
+            history.append(dict(P=P.copy(), V=V.copy(), **last))
+        if residual_tol is not None and res < residual_tol:
+            break
+    return dict(P=P, V=V, dens=dens, E=E, Etot=Etot, logs=logs, geometry=g, tables=T, LR=LR,
+                history=history, **last)
+
+
+# ---------------------------------------------------------------------------
+# Spin-polarised path (numS = 2; Main.f90:290-342, 365-595; HartreeFock.f90:929-1004)
+# Spin-resolved arrays are stacked on a leading spin axis: P[sp, c, i, j] is zFock(i+1, j+1, c+1, sp+1),
+# dens[sp, i] is Density(i+1, sp+1), V[sp, i] is Potential(i+1, sp+1).
+# ---------------------------------------------------------------------------
+def window_sort_2spins(s: Setup) -> np.ndarray:
+    """nWindowSort_2Spins of Main.f90:416-419: W[i, sp] = W(i+1, sp+1) = (NP - 1, NP + 3) for both spins."""
+    NP = s.NeutralityPoint
+    return np.array([[NP - 1, NP - 1], [NP + 3, NP + 3]], dtype=np.int64)
+
+
+def sort_energies_2spins(numk: int, numb: int, window, se1, se2):
+    """SortEnergies_2Spins (HartreeFock.f90:929-1004): merges the two spin-sorted lists.
+
+    Returns (energies, spin labels 1/2), each of length 2*numb*numk**2.  The first (W(1,1)-1)*Nk
+    spin-1 states and (W(1,2)-1)*Nk spin-2 states are copied in front without merging; the states up
+    to Nk*(W(2,sp)-1) are merged (runs may extend past that bound); the remaining spin-1 tail and
+    then the spin-2 tail are appended unmerged.  As in the reference, the front copy of spin 2 reads
+    the spin-2 list at the spin-1 counter (HartreeFock.f90:949), so every entry it writes is the
+    spin-2 energy at position (W(1,1)-1)*Nk+1; only the labels of that block are per state.
+    """
+    W = np.asarray(window, dtype=np.int64)
+    Nk = numk * numk
+    n = numb * Nk
+    se1 = np.asarray(se1, dtype=np.float64)
+    se2 = np.asarray(se2, dtype=np.float64)
+    out_e = np.zeros(2 * n)
+    out_s = np.zeros(2 * n, dtype=np.int64)
+    cb = 0
+
+    def put(e, sp):
+        nonlocal cb
+        out_e[cb] = e
+        out_s[cb] = sp
+        cb += 1
+
+    c1 = c2 = 1                                   # 1-based counters ncount1, ncount2
+    for _ in range((int(W[0, 0]) - 1) * Nk):
+        put(se1[c1 - 1], 1)
+        c1 += 1
+    for _ in range((int(W[0, 1]) - 1) * Nk):
+        put(se2[c1 - 1], 2)
+        c2 += 1
+    lim1, lim2 = Nk * (int(W[1, 0]) - 1), Nk * (int(W[1, 1]) - 1)
+    while c1 <= lim1 and c2 <= lim2:
+        if se1[c1 - 1] <= se2[c2 - 1]:
+            put(se1[c1 - 1], 1)
+            c1 += 1
+            while c1 <= n and se1[c1 - 1] <= se2[c2 - 1]:
+                put(se1[c1 - 1], 1)
+                c1 += 1
+            put(se2[c2 - 1], 2)
+            c2 += 1
+        else:
+            put(se2[c2 - 1], 2)
+            c2 += 1
+            while c2 <= n and se2[c2 - 1] <= se1[c1 - 1]:
+                put(se2[c2 - 1], 2)
+                c2 += 1
+            put(se1[c1 - 1], 1)
+            c1 += 1
+    while c1 <= n:
+        put(se1[c1 - 1], 1)
+        c1 += 1
+    while c2 <= n:
+        put(se2[c2 - 1], 2)
+        c2 += 1
+    return out_e, out_s
+
+
+def fermi_level_2spins(s: Setup, merged_e, labels):
+    """Main.f90:421-453: nFermiLevel, FermiEnergy, nOccStates(2), nPartOccStates(2), DegFactor.
+
+    Occupations are counted per spin label over the merged list; DegFactor is 0 when neither spin has
+    a partially occupied state.
+    """
+    Nk = s.Nk
+    nF = s.numS * fortran_nint(float(Nk * s.NeutralityPoint) + float(Nk) / 2.0 * s.nfilling)
+    EF = (merged_e[nF - 1] + merged_e[nF]) / 2.0
+    tol = s.EnergyTolerance
+    nocc = [0, 0]
+    npart = [0, 0]
+    for e, sp in zip(merged_e, labels):
+        k = 0 if sp == 1 else 1
+        if (e - EF) < -tol:
+            nocc[k] += 1
+        elif abs(e - EF) < tol:
+            nocc[k] += 1
+            npart[k] += 1
+    if npart[0] != 0 or npart[1] != 0:
+        deg = 1.0 / float(npart[0] + npart[1]) * float(nF + npart[0] + npart[1] - nocc[0] - nocc[1])
+    else:
+        deg = 0.0
+    return nF, EF, nocc, npart, deg
+
+
+def energies_2spins(s: Setup, T: PairTables, LR, P, dens) -> Energies:
+    """Main.f90:300-310 / OptimalStep for numS=2: kinetic and Fock energies summed over the spins,
+    Hartree and Hubbard from (n_1 - 1/2, n_2 - 1/2)."""
+    kin = sum(kinetic_energy(s, T, P[sp]) for sp in range(2))
+    fock = sum(fock_energy(s, T, P[sp]) for sp in range(2))
+    eh, eu = hartree_hubbard_energy(LR, dens[0] - 0.5, dens[1] - 0.5)
+    return Energies(kin, fock, eh, eu)
+
+
+def potential_2spins(s: Setup, LR, dens) -> np.ndarray:
+    """Main.f90:331-341 / 586-594: V_1 = alphaH LR (n_1 + n_2 - 1) + U (n_2 - 1/2), V_2 likewise with
+    U (n_1 - 1/2)."""
+    h = s.alphaH * (LR @ (dens[0] + dens[1] - 1.0))
+    return np.stack([h + s.U * (dens[1] - 0.5), h + s.U * (dens[0] - 0.5)])
+
+
+def plain_guess_2spins(s: Setup, g: Geometry, T: PairTables):
+    """Main.f90:236-292 with numS=2: the spin-1 guess of ``plain_guess``, copied to spin 2."""
+    P1, info = plain_guess(s, g, T)
+    return np.stack([P1, P1.copy()]), info
+
+
+def _density_2spins(P) -> np.ndarray:
+    return np.stack([np.real(np.diagonal(P[sp, 0])).copy() for sp in range(2)])
+
+
+def run_scf_2spins(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTables] = None, LR=None,
+                   P_init=None, itmax: Optional[int] = None, residual_tol: Optional[float] = None,
+                   keep_history: bool = False):
+    """Main.f90:236-679 for numS=2 with ODA mixing and no symmetry enforcement.
+
+    Per iteration: both spins are solved with their own potential and density matrix, sorted, merged
+    by ``sort_energies_2spins``, occupied by ``fermi_level_2spins`` (one Fermi level and DegFactor,
+    per-spin counts), projected per spin, and mixed with one OptimalStep over the spin-summed energy.
+    ``P_init`` (2, nnc, N, N) replaces the plain guess.  The residual is the largest of the per-spin
+    mean-field residuals; ``dn`` in the logs is the largest per-spin max|dn| (DensityConvergence).
+    """
+    if s.numS != 2:
+        raise ValueError("run_scf_2spins needs numS = 2")
+    if g is None:
+        g = build_geometry(s)
+    if T is None:
+        T = pair_tables(s, g)
+    if LR is None:
+        LR = long_range_interaction(s, g)
+    if P_init is None:
+        P, _ = plain_guess_2spins(s, g, T)
+    else:
+        P = np.array(P_init, dtype=np.complex128)
+    dens = _density_2spins(P)
+    E = energies_2spins(s, T, LR, P, dens)
+    Etot = E.total(s)
+    V = potential_2spins(s, LR, dens)
+    dens_in = dens.copy()
+    P_in = P.copy()
+    W = window_sort_2spins(s)
+    logs = []
+    history = []
+    itmax = s.itmax if itmax is None else itmax
+    last = {}
+    it = 0
+    while it < itmax:
+        it += 1
+        sols, ses, movs = [], [], []
+        for sp in range(2):
+            sol = solve(s, g, T, V[sp], P[sp])
+            se, _, moms, sv, _, _ = sort_energies_1spin(s, g, sol["bands"], sol["evecs"])
+            sols.append(sol)
+            ses.append(se)
+            movs.append((moms, sv))
+        me, ml = sort_energies_2spins(s.numk, s.numb, W, ses[0], ses[1])
+        nF, EF, nocc, npart, degf = fermi_level_2spins(s, me, ml)
+        P_new = np.stack([(get_fock(s, g, movs[sp][1], movs[sp][0], nocc[sp], npart[sp], degf)
+                           + sols[sp]["bulk"]) / complex(float(s.Nk), 0.0) for sp in range(2)])
+        E_in, Etot_in = E, Etot
+        dens_new = _density_2spins(P_new)
+        step, E, t1, t2 = optimal_step(s, T, LR, P_new, P_in, dens_new, dens_in, E_in,
+                                       energy_fn=energies_2spins)
+        Etot = E.total(s)
+        P = step * P_new + (1.0 - step) * P_in
+        dens = _density_2spins(P)
+        dn = float(np.max(np.abs(dens - dens_in)))
+        V_old = V
+        V = potential_2spins(s, LR, dens)
+        res = max(hf_residual(s, T, V[sp], V_old[sp], P[sp], P_in[sp]) for sp in range(2))
+        dens_in = dens.copy()
+        P_in = P.copy()
+        logs.append(IterationLog(it, dn, step, Etot_in - Etot, Etot_in, E_in.kinetic, E_in.fock,
+                                 E_in.hartree, E_in.hubbard, EF, nocc[0] + nocc[1], npart[0] + npart[1], res))
+        last = dict(bands=np.stack([x["bands"] for x in sols]), EF=EF, nocc=nocc, npart=npart, degf=degf,
+                    merged=(me, ml), P_new=P_new, step=step, E1=t1, Ehalf=t2)
         if keep_history:
             history.append(dict(P=P.copy(), V=V.copy(), **last))
         if residual_tol is not None and res < residual_tol:

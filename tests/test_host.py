@@ -162,3 +162,46 @@ def test_rayleigh_ritz_small_solve_matches_numpy(n, seed):
     assert np.all(np.diff(th) >= 0)
     assert np.max(np.abs(G @ M - S @ M * th)) <= 1e-11 * scale
     assert np.max(np.abs(M.conj().T @ S @ M - np.eye(n))) <= 1e-12
+
+
+def test_host_sort_energies_2spins_matches_oracle(lib):
+    import forge_gb300 as fg
+    # the hand-worked lists of the oracle tests, then random per-spin sorted lists with ties
+    se1 = [0.0, 1.0, 2.0, 3.0, 4.0, 5.0]
+    se2 = [10.0, 0.5, 1.5, 2.5, 3.5, 4.5]
+    out = fg.sort_energies_2spins(1, 6, [[2, 2], [5, 5]], np.stack([se1, se2], 1))
+    e, lab = fo.sort_energies_2spins(1, 6, [[2, 2], [5, 5]], se1, se2)
+    assert np.array_equal(out[:, 0], e) and np.array_equal(out[:, 1], lab)
+    rng = np.random.default_rng(11)
+    for numk, numb, W in ((2, 20, [[9, 9], [13, 13]]), (3, 20, [[9, 9], [13, 13]]), (1, 14, [[1, 1], [15, 15]]),
+                          (2, 8, [[3, 2], [6, 9]])):
+        n = numb * numk * numk
+        se = np.sort(np.round(rng.normal(size=(n, 2)), 1), axis=0)      # rounding makes equal energies
+        out = fg.sort_energies_2spins(numk, numb, W, se)
+        e, lab = fo.sort_energies_2spins(numk, numb, np.array(W), se[:, 0], se[:, 1])
+        assert np.array_equal(out[:, 0], e) and np.array_equal(out[:, 1], lab), (numk, numb, W)
+
+
+def test_host_sort_energies_2spins_rejects_windows_outside_the_lists(lib):
+    import forge_gb300 as fg
+    se = np.zeros((6, 2))
+    for W in ([[0, 1], [3, 3]], [[3, 1], [2, 3]], [[2, 2], [8, 3]], [[7, 2], [7, 7]]):
+        with pytest.raises(fg.ForgeError):
+            fg.sort_energies_2spins(1, 6, np.array(W), se)
+
+
+@pytest.mark.parametrize("nfilling,split", [(0.0, 0.3), (2.0, 0.0), (-1.5, 0.05), (1.0, 0.0)])
+def test_host_fermi_2spins_matches_oracle(lib, nfilling, split):
+    import forge_gb300 as fg
+    s = fg.Setup(ntheta=1, numk=3, nfilling=nfilling, numS=2)
+    so = fo.Setup(ntheta=1, numk=3, nfilling=nfilling, numS=2)
+    n = so.numb * so.Nk
+    rng = np.random.default_rng(5)
+    base = np.sort(np.round(rng.normal(size=n), 2))
+    se = np.stack([base, np.sort(base + split * rng.normal(size=n))], 1)
+    r = fg.fermi_2spins(s, se)
+    e, lab = fo.sort_energies_2spins(so.numk, so.numb, fo.window_sort_2spins(so), se[:, 0], se[:, 1])
+    nF, EF, nocc, npart, deg = fo.fermi_level_2spins(so, e, lab)
+    assert np.array_equal(r["SortedEnergies_2Spins"][:, 0], e)
+    assert (r["nFermiLevel"], r["FermiEnergy"], r["nOccStates"], r["nPartOccStates"]) == (nF, EF, nocc, npart)
+    assert r["DegFactor"] == deg
