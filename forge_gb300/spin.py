@@ -1,0 +1,188 @@
+"""Spin-polarised SCF (numS = 2) on two device contexts, one per spin.
+
+Main.f90:236-679 with numS = 2 and no symmetry enforcement.  Each spin has its own context.  That
+context holds the spin's density matrix, solves H(k) with the spin's potential, and forms the
+spin's new density matrix.  These are the per-spin routines of the numS = 1 path, unchanged.  The
+host joins the spins:
+- it merges the two sorted band lists and sets one Fermi level (forge_host_fermi_2spins);
+- it sums the kinetic and Fock energies over the spins;
+- it evaluates the Hartree and Hubbard terms from both densities;
+- it takes one OptimalStep for both spins;
+- it builds each spin's potential from both densities (Main.f90:586-594).
+
+Density matrices cross the host boundary once per energy evaluation.  This path is for correctness
+and for systems of moderate size; it is not the benchmarked path.
+
+Arrays follow the reference: zFock(ndim, ndim, numNeighborCells) per spin, column-major.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import Optional, Sequence
+
+import numpy as np
+
+from .api import Geometry, HartreeFock, Setup, build_geometry, fermi_2spins
+
+
+@dataclasses.dataclass
+class SpinIteration:
+    """One line of the Convergence / Energy output of Main.f90:612-625 for numS = 2."""
+
+    it: int
+    DensityConvergence: float       # max over spins of max_n |n_new - n_old|
+    Step: float
+    TotalEnergyIn: float
+    TotalEnergy: float
+    FermiEnergy: float
+    nOccStates: tuple
+    nPartOccStates: tuple
+    DegFactor: float
+
+
+def hartree_hubbard(LR: np.ndarray, dens: Sequence[np.ndarray]) -> tuple:
+    """GetHartreeHubbardEnergy (HartreeFock.f90:1066-1092) with dens1 = n_1 - 1/2, dens2 = n_2 - 1/2."""
+    d1, d2 = dens[0] - 0.5, dens[1] - 0.5
+    sm = d1 + d2
+    return 0.5 * float(sm @ (LR @ sm)), float(np.dot(d1, d2))
+
+
+def potentials(LR: np.ndarray, dens: Sequence[np.ndarray], alphaH: float, U: float) -> list:
+    """Main.f90:331-341 / 586-594: V_1 = alphaH LR (n_1 + n_2 - 1) + U (n_2 - 1/2), V_2 with U (n_1 - 1/2)."""
+    h = alphaH * (LR @ (dens[0] + dens[1] - 1.0))
+    return [h + U * (dens[1] - 0.5), h + U * (dens[0] - 0.5)]
+
+
+def density(zFock: np.ndarray) -> np.ndarray:
+    """Density(:, spin) = real(zFock(n, n, 1, spin)) (Main.f90:294-298)."""
+    return np.ascontiguousarray(np.real(np.diagonal(zFock[:, :, 0])))
+
+
+class SpinPolarisedScf:
+    """Main.f90:236-679 for numS = 2 with ODA mixing.
+
+    ``setup.numS`` must be 2.  ``engines`` are the two per-spin engines.  They default to device
+    contexts (``HartreeFock`` of the same setup with numS = 1).  Another object with the same
+    methods may stand in, for instance a CPU model of the routines in a test.
+    """
+
+    def __init__(self, setup: Setup, geometry: Optional[Geometry] = None, engines: Optional[Sequence] = None):
+        if setup.numS != 2:
+            raise ValueError("SpinPolarisedScf needs numS = 2")
+        self.setup = setup
+        self.s = setup.to_struct()
+        one = dataclasses.replace(setup, numS=1)
+        if engines is None:
+            g = geometry if geometry is not None else build_geometry(one)
+            engines = [HartreeFock(one, g), HartreeFock(one, g)]
+            self._own = True
+        else:
+            self._own = False
+        self.hf = list(engines)
+        self.LR = np.asarray(self.hf[0].LongRangeInteraction())
+        self.hf[1].LongRangeInteraction(copy_out=False)
+        self.P = None
+        self.dens = None
+        self.V = None
+        self.E = None
+
+    def close(self):
+        if self._own:
+            for h in self.hf:
+                h.close()
+        self.hf = []
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- energies of a spin pair of density matrices (Main.f90:300-312, OptimalStep's evaluations)
+    def energies(self, P: Sequence[np.ndarray], dens: Sequence[np.ndarray]) -> tuple:
+        kin = fock = 0.0
+        for sp in range(2):
+            k, f, _, _ = self.hf[sp].Energies(P[sp])
+            kin += k
+            fock += f
+        eh, eu = hartree_hubbard(self.LR, dens)
+        return kin, fock, eh, eu
+
+    def total(self, E: Sequence[float]) -> float:
+        """TotalEnergy of Main.f90:312 with the factor 3 - numS = 1."""
+        s = self.s
+        return s.alpha * E[1] + E[0] + s.U * E[3] + s.alphaH * E[2]
+
+    # -- initial state
+    def plain_guess(self):
+        """Main.f90:236-292 with numS = 2: the non-interacting spin-1 guess, copied to spin 2."""
+        E, info = self.hf[0].PlainGuess()
+        P1, _, _ = self.hf[0].GetState()
+        self.set_state([P1, P1.copy()])
+        return info
+
+    def set_state(self, P: Sequence[np.ndarray]):
+        """Loads both spins' zFock and forms their energies and potentials (Main.f90:294-346)."""
+        self.P = [np.asfortranarray(np.asarray(p, dtype=np.complex128)) for p in P]
+        for sp in range(2):
+            self.hf[sp].SetState(self.P[sp])
+        self.dens = [density(p) for p in self.P]
+        self.E = self.energies(self.P, self.dens)
+        self.V = potentials(self.LR, self.dens, self.s.alphaH, self.s.U)
+
+    # -- one SCF iteration (Main.f90:365-595)
+    def iterate(self, it: int = 0) -> SpinIteration:
+        if self.P is None:
+            raise RuntimeError("no state: call plain_guess() or set_state() first")
+        s = self.s
+        sorted_e = []
+        for sp in range(2):
+            _, _, _, info = self.hf[sp].Solve(self.V[sp], None, bands=False)
+            if info > 0:
+                print("zheev failed", info)           # LapackRoutines.f90:430 behaviour
+            e, _, _ = self.hf[sp].SortEnergies_1Spin()
+            sorted_e.append(e)
+        fl = fermi_2spins(self.setup, np.stack(sorted_e, 1))
+        deg = fl["DegFactor"]
+        nocc, npart = fl["nOccStates"], fl["nPartOccStates"]
+        Pn = [self.hf[sp].GetFock(deg, nocc[sp], npart[sp]) for sp in range(2)]
+        dn_new = [density(p) for p in Pn]
+        # OptimalStep (HartreeFock.f90:1148-1227) over the spin-summed energy
+        c0 = self.total(self.E)
+        t1 = self.total(self.energies(Pn, dn_new))
+        half = [0.5 * (self.P[sp] + Pn[sp]) for sp in range(2)]
+        t2 = self.total(self.energies(half, [0.5 * (self.dens[sp] + dn_new[sp]) for sp in range(2)]))
+        c1 = 4.0 * t2 - t1 - 3.0 * c0
+        c2 = t1 - c0 - c1
+        if c2 > 0 and abs(-c1 / 2.0 / c2 - .5) < 0.5:
+            step = -c1 / 2.0 / c2
+        elif t1 < c0:
+            step = 1.0
+        else:
+            step = s.StepAlternative
+        P = [step * Pn[sp] + (1.0 - step) * self.P[sp] for sp in range(2)]
+        dens = [density(p) for p in P]
+        E = self.energies(P, dens)
+        dn = max(float(np.max(np.abs(dens[sp] - self.dens[sp]))) for sp in range(2))
+        Ein = self.E
+        self.P, self.dens, self.E = P, dens, E
+        for sp in range(2):
+            self.hf[sp].SetState(P[sp])
+        self.V = potentials(self.LR, dens, s.alphaH, s.U)
+        return SpinIteration(it, dn, step, self.total(Ein), self.total(E), fl["FermiEnergy"], tuple(nocc),
+                             tuple(npart), deg)
+
+    def run(self, itmax: int, density_tol: float = 0.0, P_init: Optional[Sequence[np.ndarray]] = None) -> list:
+        """The SCF loop: itmax iterations (the reference's stop), or fewer once DensityConvergence
+        drops below ``density_tol`` (> 0)."""
+        if P_init is not None:
+            self.set_state(P_init)
+        elif self.P is None:
+            self.plain_guess()
+        reports = []
+        for it in range(1, itmax + 1):
+            r = self.iterate(it)
+            reports.append(r)
+            if density_tol > 0 and r.DensityConvergence < density_tol:
+                break
+        return reports

@@ -50,7 +50,8 @@ typedef struct forge_setup {
     int64_t nlayers;          /* Setup.f90:7 */
     int64_t ntheta;           /* Setup.f90:8 */
     int64_t numk;             /* Setup.f90:11 */
-    int64_t numS;             /* Setup.f90:13 (only 1 is supported) */
+    int64_t numS;             /* Setup.f90:13: a context holds one spin (1); numS = 2 runs one context per
+                                 spin joined on the host (forge_host_fermi_2spins) */
     int64_t numI;             /* Setup.f90:19 (only 1 is supported: 4 neighbour cells) */
     int64_t numC;             /* Setup.f90:20 */
     int64_t nscreen;          /* Setup.f90:21 */

@@ -1,0 +1,95 @@
+"""CPU test of the two-spin SCF host logic (forge_gb300.spin): with each per-spin device context
+replaced by a CPU model of the same routines (the oracle's Solve, SortEnergies_1Spin, GetFock and
+energy functions), SpinPolarisedScf must follow the oracle's numS = 2 SCF (run_scf_2spins).  The
+merge and Fermi level run in the library's host code (forge_host_fermi_2spins)."""
+import numpy as np
+import pytest
+
+from oracle import forge_oracle as fo
+
+
+def _to_P(Pf):
+    return np.ascontiguousarray(np.moveaxis(Pf, 2, 0))
+
+
+def _to_F(P):
+    return np.asfortranarray(np.moveaxis(P, 0, 2))
+
+
+class OracleSpinEngine:
+    """CPU model of one per-spin device context: the HartreeFock methods SpinPolarisedScf calls."""
+
+    def __init__(self, so, g, T, LR):
+        self.so, self.g, self.T, self.LR = so, g, T, LR
+        self.P = np.zeros((4, so.ndim, so.ndim), complex)
+        self.sol = None
+        self.sorted = None
+
+    def LongRangeInteraction(self, copy_out=True):
+        return self.LR.copy() if copy_out else None
+
+    def PlainGuess(self):
+        self.P, _ = fo.plain_guess(self.so, self.g, self.T)
+        return (0.0, 0.0, 0.0, 0.0), 0
+
+    def GetState(self):
+        return _to_F(self.P), np.real(np.diagonal(self.P[0])).copy(), None
+
+    def SetState(self, zFock):
+        self.P = _to_P(zFock)
+
+    def Energies(self, zFock=None):
+        P = self.P if zFock is None else _to_P(zFock)
+        return fo.kinetic_energy(self.so, self.T, P), fo.fock_energy(self.so, self.T, P), 0.0, 0.0
+
+    def Solve(self, Potential=None, zFock=None, bands=True, vectors=False, bulk=False):
+        self.sol = fo.solve(self.so, self.g, self.T, np.asarray(Potential), self.P)
+        return None, None, None, 0
+
+    def SortEnergies_1Spin(self):
+        se, idx, moms, sv, _, _ = fo.sort_energies_1spin(self.so, self.g, self.sol["bands"], self.sol["evecs"])
+        self.sorted = (moms, sv)
+        return se, moms, idx
+
+    def GetFock(self, DegFactor, nOccStates, nPartOccStates, copy_out=True):
+        moms, sv = self.sorted
+        Pw = fo.get_fock(self.so, self.g, sv, moms, nOccStates, nPartOccStates, DegFactor)
+        return _to_F((Pw + self.sol["bulk"]) / complex(float(self.so.Nk), 0.0))
+
+
+@pytest.mark.parametrize("split", [False, True])
+def test_spin_scf_host_logic_follows_the_oracle(lib, split):
+    import forge_gb300 as fg
+    from forge_gb300.spin import SpinPolarisedScf
+    kw = dict(ntheta=1, numk=3, nfilling=2.0, degfactor_mode="corrected")
+    so1 = fo.Setup(**kw)
+    so2 = fo.Setup(numS=2, **kw)
+    g = fo.build_geometry(so1)
+    T = fo.pair_tables(so1, g)
+    LR = fo.long_range_interaction(so1, g)
+    P0 = None
+    if split:
+        P0 = np.stack([fo.plain_guess(fo.Setup(**{**kw, "nfilling": kw["nfilling"] + d}), g, T)[0]
+                       for d in (1.0, -1.0)])
+    ref = fo.run_scf_2spins(so2, g, T, LR, P_init=P0, itmax=3)
+    engines = [OracleSpinEngine(so1, g, T, LR) for _ in range(2)]
+    scf = SpinPolarisedScf(fg.Setup(numS=2, **kw), engines=engines)
+    reps = scf.run(3, P_init=None if P0 is None else [_to_F(p) for p in P0])
+    assert len(reps) == len(ref["logs"]) == 3
+    for r, l in zip(reps, ref["logs"]):
+        assert r.TotalEnergyIn == pytest.approx(l.E_in, abs=1e-10)
+        assert r.Step == pytest.approx(l.step, abs=1e-12)
+        assert r.DensityConvergence == pytest.approx(l.dn_max, abs=1e-12)
+        assert sum(r.nOccStates) == l.nocc and sum(r.nPartOccStates) == l.npart
+        assert r.FermiEnergy == l.EF
+    for sp in range(2):
+        assert np.max(np.abs(_to_P(scf.P[sp]) - ref["P"][sp])) <= 1e-12
+        assert np.max(np.abs(scf.V[sp] - ref["V"][sp])) <= 1e-11
+    assert scf.total(scf.E) == pytest.approx(ref["Etot"], abs=1e-10)
+
+
+def test_spin_scf_rejects_numS1(lib):
+    import forge_gb300 as fg
+    from forge_gb300.spin import SpinPolarisedScf
+    with pytest.raises(ValueError):
+        SpinPolarisedScf(fg.Setup(ntheta=1, numk=3), engines=[None, None])
