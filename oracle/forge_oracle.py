@@ -45,7 +45,8 @@ class Setup:
     degenerate states are weighted in GetFock: ``"reference"`` reproduces
     ``zdeg = cmplx(DegFactor, dp)`` (HartreeFock.f90:529) literally, i.e. the
     single-precision real part and an imaginary part equal to ``dp`` = 8;
-    ``"corrected"`` uses the real weight DegFactor.
+    ``"corrected"`` uses the real weight DegFactor.  ``nenforceC3 = 1`` (Setup.f90:27) selects
+    Solve_C3 / GetFock_C3 in the SCF drivers.
     """
 
     ntheta: int = 5
@@ -66,6 +67,7 @@ class Setup:
     StepAlternative: float = 1.0
     pressure: float = 1.0
     numS: int = 1
+    nenforceC3: int = 0
     degfactor_mode: str = "reference"
 
     # derived (Setup.f90:10, 23-24, 58-69)
@@ -744,6 +746,182 @@ def get_fock(s: Setup, g: Geometry, sorted_vecs, moms, nocc: int, npart: int, de
 
 
 # ---------------------------------------------------------------------------
+# C3-reduced solve and projector (nenforceC3 = 1; HartreeFock.f90:131-398, 564-881)
+# ---------------------------------------------------------------------------
+def c3_invariant(numk: int, icount: int) -> bool:
+    """The k points Solve_C3 / GetFock_C3 treat as C3-invariant (HartreeFock.f90:219, 588): icount 1,
+    numk/3*(numk+1)+1 and 2*numk/3*(numk+1)+1 (1-based, integer division).  These are the invariant
+    points of the grid only when numk is a multiple of 3."""
+    return icount in (1, numk // 3 * (numk + 1) + 1, 2 * numk // 3 * (numk + 1) + 1)
+
+
+def c3_related_momenta(s: Setup, g: Geometry) -> np.ndarray:
+    """C3_RelatedMomenta (HartreeFock.f90:151-166): (Nk, 3) 1-based icounts of k, C3 k and C3^2 k,
+    icount = ivk1*numk + ivk2 + 1."""
+    numk = s.numk
+    rel = np.zeros((s.Nk, 3), dtype=np.int64)
+    for ic in range(1, s.Nk + 1):
+        a, b = (int(x) for x in g.kcomp[ic - 1])
+        rel[ic - 1, 0] = ic
+        rel[ic - 1, 1] = ((-a - b) % numk) * numk + (a % numk) + 1
+        rel[ic - 1, 2] = (b % numk) * numk + ((-a - b) % numk) + 1
+    return rel
+
+
+def c3_representatives(s: Setup, rel: np.ndarray) -> list:
+    """MomentaMod_C3 (HartreeFock.f90:168-187): the first k of every C3 orbit, in icount order."""
+    included = set()
+    reps = []
+    for ic in range(1, s.Nk + 1):
+        if ic not in included:
+            reps.append(ic)
+            included.update((ic, int(rel[ic - 1, 1]), int(rel[ic - 1, 2])))
+    return reps
+
+
+def _corner_sites(s: Setup):
+    """(0-based index of site ndim/nlayers*(l-1) + ndim/nlayers/2, of site ndim/nlayers*l, RotateLayers(l))."""
+    per = s.ndim // s.nlayers
+    return [(per * l + per // 2 - 1, per * (l + 1) - 1, int(s.RotateLayers[l])) for l in range(s.nlayers)]
+
+
+def _c3_vector_phase(s: Setup, q: int) -> np.ndarray:
+    """zphase of the C3-rotated eigenvectors for fphase = 0 (HartreeFock.f90:223-235, 249-261): 1 except
+    exp(-+2 pi i q/numk) on the two corner sites of each layer (sign by RotateLayers)."""
+    z = np.ones(s.ndim, dtype=np.complex128)
+    th = 2 * PI * float(q) / float(s.numk)
+    for ih, ie, rot in _corner_sites(s):
+        if rot == -1:
+            z[ih], z[ie] = np.exp(complex(0.0, -th)), np.exp(complex(0.0, th))
+        elif rot == 1:
+            z[ih], z[ie] = np.exp(complex(0.0, th)), np.exp(complex(0.0, -th))
+    return z
+
+
+def _c3_matrix_image(s: Setup, M: np.ndarray, p0: np.ndarray, q: int) -> np.ndarray:
+    """M(nC3pairs, nC3pairs) with the corner phases of HartreeFock.f90:303-327: for RotateLayers -1, the
+    rows of the two corner sites times exp(-i th), exp(+i th) and their columns times exp(+i th),
+    exp(-i th), th = 2 pi q/numk; the opposite signs for RotateLayers 1.  The first image takes
+    q = ivk1+ivk2, the second (applied to the first) q = -ivk1 (HartreeFock.f90:342-366)."""
+    out = M[np.ix_(p0, p0)].copy()
+    th = 2 * PI * float(abs(q)) / float(s.numk)
+    sgn = 1.0 if q >= 0 else -1.0
+    em, ep = np.exp(complex(0.0, -sgn * th)), np.exp(complex(0.0, sgn * th))
+    for ih, ie, rot in _corner_sites(s):
+        if rot == -1:
+            out[ih, :] *= em
+            out[ie, :] *= ep
+            out[:, ih] *= ep
+            out[:, ie] *= em
+        elif rot == 1:
+            out[ih, :] *= ep
+            out[ie, :] *= em
+            out[:, ih] *= em
+            out[:, ie] *= ep
+    return out
+
+
+def _c3_orbit_sum(s: Setup, g: Geometry, B1: np.ndarray, ka, kb, kc) -> np.ndarray:
+    """B1 and its two C3 images spread over the neighbour cells (HartreeFock.f90:292-372): cell c gets
+    B1 with the Bloch phase of k = ka, the first image with that of kb, the second with that of kc."""
+    nnc = len(g.ucell1)
+    p0 = g.c3pairs - 1
+    a, b = ka
+    T = np.zeros((nnc, s.ndim, s.ndim), dtype=np.complex128)
+    T[0] = B1
+    for c in range(1, nnc):
+        T[c] = B1 * bloch_phase_int(a, b, int(g.ucell1[c]), int(g.ucell2[c]), s.numk)
+    M1 = _c3_matrix_image(s, B1, p0, a + b)
+    T[0] += M1
+    for c in range(1, nnc):
+        T[c] += M1 * bloch_phase_int(kb[0], kb[1], int(g.ucell1[c]), int(g.ucell2[c]), s.numk)
+    M2 = _c3_matrix_image(s, M1, p0, -a)
+    T[0] += M2
+    for c in range(1, nnc):
+        T[c] += M2 * bloch_phase_int(kc[0], kc[1], int(g.ucell1[c]), int(g.ucell2[c]), s.numk)
+    return T
+
+
+def solve_c3(s: Setup, g: Geometry, T: PairTables, potential, P):
+    """Solve_C3 (HartreeFock.f90:131-398), fphase = 0: one eigen-solve per C3 orbit of k points.
+
+    The bands of the orbit's representative are copied to the two rotated k; for orbits of three
+    points, the eigenvectors of C3 k and C3^2 k are the representative's permuted by nC3pairs twice
+    and once, with the corner phases of _c3_vector_phase.  The bulk projector of the representative
+    is added with its two C3 images (the third of the sum for the invariant points).  Returns the
+    dict of ``solve``.  numk must be a multiple of 3: for other numk the reference treats k points
+    that are not C3-invariant as invariant and leaves the eigenvectors of their orbit unset.
+    """
+    if s.numk % 3 != 0:
+        raise ValueError("Solve_C3 needs numk divisible by 3")
+    if s.fphase != 0:
+        raise ValueError("the C3-reduced solve is restated for fphase = 0")
+    N, Nk, numb, numk = s.ndim, s.Nk, s.numb, s.numk
+    nL, nU = s.nLower, s.nUpper
+    nnc = T.tm.shape[0]
+    rel = c3_related_momenta(s, g)
+    p0 = g.c3pairs - 1
+    bands = np.zeros((numb, Nk))
+    evecs = np.zeros((N, numb, Nk), dtype=np.complex128)
+    bulk = np.zeros((nnc, N, N), dtype=np.complex128)
+    allw = np.zeros((nU, Nk))
+    for ic in c3_representatives(s, rel):
+        a, b = (int(x) for x in g.kcomp[ic - 1])
+        k2, k3 = int(rel[ic - 1, 1]), int(rel[ic - 1, 2])
+        H = hamiltonian(s, g, T, potential, P, g.kvals[a, b])
+        w, Z = eigh_lower(H, nU)
+        for kk in (ic, k2, k3):
+            bands[:, kk - 1] = w[nL - 1:nU]
+            allw[:, kk - 1] = w
+        evecs[:, :, ic - 1] = Z[:, nL - 1:nU]
+        inv = c3_invariant(numk, ic)
+        if not inv:
+            c2a, c2b = (int(x) for x in g.kcomp[k2 - 1])
+            c3b = int(g.kcomp[k3 - 1][1])
+            evecs[:, :, k2 - 1] = Z[p0[p0], nL - 1:nU] * _c3_vector_phase(s, c2a + c2b)[:, None]
+            evecs[:, :, k3 - 1] = Z[p0, nL - 1:nU] * _c3_vector_phase(s, c3b)[:, None]
+        occ = np.conj(Z[:, :nL - 1])
+        B1 = occ @ np.conj(occ).T
+        kb = tuple(int(x) for x in g.kcomp[k3 - 1])
+        kc = tuple(int(x) for x in g.kcomp[k2 - 1])
+        Tk = _c3_orbit_sum(s, g, B1, (a, b), kb, kc)
+        bulk += Tk / 3.0 if inv else Tk
+    return dict(bands=bands, evecs=evecs, bulk=bulk, eigs=allw)
+
+
+def get_fock_c3(s: Setup, g: Geometry, sorted_vecs, moms, nocc: int, npart: int, degf: float) -> np.ndarray:
+    """GetFock_C3 (HartreeFock.f90:564-881), fphase = 0: GetFock for states at k points that are not
+    C3-invariant; a state at an invariant k enters as the third of its projector plus its two C3
+    images (with the Bloch phase of its own k in every cell)."""
+    N = s.ndim
+    nnc = len(g.ucell1)
+    out = np.zeros((nnc, N, N), dtype=np.complex128)
+    zdeg = zdeg_weight(s, degf)
+    for rng, extra in ((range(0, nocc - npart), 1.0 + 0j), (range(nocc - npart, nocc), zdeg)):
+        for nb in rng:
+            a, b = (int(x) for x in moms[nb])
+            zp = np.conj(sorted_vecs[:, nb])
+            outer = np.outer(zp, np.conj(zp))
+            if not c3_invariant(s.numk, a * s.numk + b + 1):
+                for c in range(nnc):
+                    out[c] += outer * (bloch_phase_int(a, b, int(g.ucell1[c]), int(g.ucell2[c]), s.numk) * extra)
+            else:
+                out += _c3_orbit_sum(s, g, outer * extra, (a, b), (a, b), (a, b)) / complex(3.0, 0.0)
+    return out
+
+
+def solve_any(s: Setup, g: Geometry, T: PairTables, potential, P):
+    """Solve or Solve_C3 by nenforceC3 (Main.f90:244-250, 375-381)."""
+    return solve_c3(s, g, T, potential, P) if s.nenforceC3 == 1 else solve(s, g, T, potential, P)
+
+
+def get_fock_any(s: Setup, g: Geometry, sorted_vecs, moms, nocc: int, npart: int, degf: float) -> np.ndarray:
+    """GetFock or GetFock_C3 by nenforceC3 (Main.f90:273-279, 502-508)."""
+    f = get_fock_c3 if s.nenforceC3 == 1 else get_fock
+    return f(s, g, sorted_vecs, moms, nocc, npart, degf)
+
+
+# ---------------------------------------------------------------------------
 # Energies, ODA step, potential (HartreeFock.f90:1012-1227, Main.f90:300-342, 549-595)
 # ---------------------------------------------------------------------------
 def kinetic_energy(s: Setup, T: PairTables, P) -> float:
@@ -871,10 +1049,10 @@ def plain_guess(s: Setup, g: Geometry, T: PairTables):
     nnc = len(g.ucell1)
     P0 = np.zeros((nnc, N, N), dtype=np.complex128)
     V0 = np.zeros(N)
-    sol = solve(s, g, T, V0, P0)
+    sol = solve_any(s, g, T, V0, P0)
     se, _, moms, sv, _, _ = sort_energies_1spin(s, g, sol["bands"], sol["evecs"])
     nF, EF, nocc, npart, degf = fermi_level(s, se, spin_factor=1)
-    P = get_fock(s, g, sv, moms, nocc, npart, degf)
+    P = get_fock_any(s, g, sv, moms, nocc, npart, degf)
     P = (P + sol["bulk"]) / complex(float(s.Nk), 0.0)
     return P, dict(sol=sol, EF=EF, nocc=nocc, npart=npart, degf=degf)
 
@@ -957,10 +1135,10 @@ def run_scf(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTables] = No
     last = {}
     while it < itmax:
         it += 1
-        sol = solve(s, g, T, V, P)
+        sol = solve_any(s, g, T, V, P)
         se, _, moms, sv, _, _ = sort_energies_1spin(s, g, sol["bands"], sol["evecs"])
         nF, EF, nocc, npart, degf = fermi_level(s, se)
-        Pw = get_fock(s, g, sv, moms, nocc, npart, degf)
+        Pw = get_fock_any(s, g, sv, moms, nocc, npart, degf)
         P_new = (Pw + sol["bulk"]) / complex(float(s.Nk), 0.0)
         E_in, Etot_in = E, Etot
         dens_new = np.real(np.diagonal(P_new[0])).copy()
@@ -1157,14 +1335,14 @@ def run_scf_2spins(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTable
         it += 1
         sols, ses, movs = [], [], []
         for sp in range(2):
-            sol = solve(s, g, T, V[sp], P[sp])
+            sol = solve_any(s, g, T, V[sp], P[sp])
             se, _, moms, sv, _, _ = sort_energies_1spin(s, g, sol["bands"], sol["evecs"])
             sols.append(sol)
             ses.append(se)
             movs.append((moms, sv))
         me, ml = sort_energies_2spins(s.numk, s.numb, W, ses[0], ses[1])
         nF, EF, nocc, npart, degf = fermi_level_2spins(s, me, ml)
-        P_new = np.stack([(get_fock(s, g, movs[sp][1], movs[sp][0], nocc[sp], npart[sp], degf)
+        P_new = np.stack([(get_fock_any(s, g, movs[sp][1], movs[sp][0], nocc[sp], npart[sp], degf)
                            + sols[sp]["bulk"]) / complex(float(s.Nk), 0.0) for sp in range(2)])
         E_in, Etot_in = E, Etot
         dens_new = _density_2spins(P_new)
