@@ -117,6 +117,7 @@ SIGNATURES = {
     "forge_host_plot_bands": [_P, _P, _D, _P, _P, _P, C.c_char_p],
     "forge_host_write_fock": [_P, _P, C.c_char_p, _I],
     "forge_host_read_fock": [_P, _P, C.c_char_p, _I],
+    "forge_gpu_set_c3": [_P, _I, _P, _P],
     "forge_host_sort_energies_2spins": [_I, _I, _P, _P, _P],
     "forge_host_fermi_2spins": [_P, _P, _P, _P, _P, _P, _P, _P],
 }
@@ -185,6 +186,7 @@ class Setup:
     xi: float = 10.0 / 0.246
     fphase: int = 0
     numS: int = 1
+    nenforceC3: int = 0
     EnergyTolerance: float = 0.0001
     StepAlternative: float = 1.0
     degfactor_mode: str = "reference"
@@ -323,6 +325,8 @@ class HartreeFock:
         _check(lib.forge_gpu_init(C.byref(self.s), *[_ptr(a) for a in self._keep], C.byref(ctx)))
         self.ctx = ctx
         self.lib = lib
+        if setup.nenforceC3:
+            self.set_c3(setup.nenforceC3)
 
     def close(self):
         if getattr(self, "ctx", None):
@@ -351,6 +355,12 @@ class HartreeFock:
     def set_refinement(self, width: int = 32):
         """FP64 Rayleigh-Ritz refinement of the top `width` bands after each mixed solve (0: off)."""
         _check(self.lib.forge_gpu_set_refinement(self.ctx, width))
+
+    def set_c3(self, nenforceC3: int = 1):
+        """nenforceC3 (Setup.f90:27): 1 = Solve_C3 / GetFock_C3, 0 = the full solve."""
+        pairs = _f(self.geometry.nC3pairs, np.int64)
+        rl = np.ascontiguousarray(self.setup.RotateLayers, dtype=np.int64)
+        _check(self.lib.forge_gpu_set_c3(self.ctx, nenforceC3, _ptr(pairs), _ptr(rl)))
 
     def set_mixing(self, mode: str = "oda", depth: int = 6, beta: float = 0.7):
         """SCF mixing: "oda" (the reference's OptimalStep) or "pulay" (Anderson / Pulay, `depth` steps)."""

@@ -107,6 +107,10 @@ struct forge_ctx {
     int diis_nslots = 0;             // slots allocated (depth + 1)
     bool diis_has_prev = false;
     double diis_G[DIIS_MAX][DIIS_MAX] = {};
+    // C3-reduced solve (forge_gpu_set_c3): H(k) solved for the first k of each C3 orbit only
+    bool c3 = false;
+    C3Tables c3t;
+    DevBuf c3_Xr, c3_wr, c3_tab, c3_perm, c3_phase;
     bool have_solve = false, have_sort = false, have_pnew = false, have_state = false, bulk_is_fused = false;
     std::vector<int64_t> h_sorted_idx;
     std::vector<double2> h_bph;
@@ -135,7 +139,8 @@ int choose_batch(forge_ctx* x) {
     cudaMemGetInfo(&freeb, &totalb);
     // kept free: 8 GB headroom, the eigenvectors of every k, the four bulk cells and the
     // projector / window work arrays allocated after the batch is chosen
-    const size_t reserve = ((size_t)8 << 30) + (size_t)c.Nk * N * iu * 16 + (size_t)10 * N * N * 16;
+    const int64_t xslots = x->c3 ? x->c3t.nslots + (int64_t)x->c3t.reps.size() : c.Nk;
+    const size_t reserve = ((size_t)8 << 30) + (size_t)xslots * N * iu * 16 + (size_t)10 * N * N * 16;
     const size_t budget = freeb > reserve ? freeb - reserve : freeb / 4;
     int64_t b = (int64_t)(budget / per_k);
     // FORGE_EIG_BATCH caps the number of k points solved per launch (memory control)
@@ -157,9 +162,16 @@ int ensure_solve_buffers(forge_ctx* x) {
     const size_t NN = (size_t)N * N;
     if (x->eig_batch == 0) x->eig_batch = choose_batch(x);
     const int64_t B = x->eig_batch;
+    // eigenvector slots: one per k, plus the two rotated copies of each C3-invariant k
+    const int64_t nslots = x->c3 ? x->c3t.nslots : Nk;
     FORGE_TRY(c.H.ensure((size_t)B * NN * sizeof(double2)));
-    FORGE_TRY(c.X.ensure((size_t)Nk * N * iu * sizeof(double2)));
-    FORGE_TRY(x->w.ensure((size_t)Nk * iu * sizeof(double)));
+    FORGE_TRY(c.X.ensure((size_t)nslots * N * iu * sizeof(double2)));
+    FORGE_TRY(x->w.ensure((size_t)nslots * iu * sizeof(double)));
+    if (x->c3) {
+        const size_t nr = x->c3t.reps.size();
+        FORGE_TRY(x->c3_Xr.ensure(nr * N * iu * sizeof(double2)));
+        FORGE_TRY(x->c3_wr.ensure(nr * iu * sizeof(double)));
+    }
     FORGE_TRY(x->eigws.ensure(eig_workspace_bytes(N, iu, B)));
     if (c.precision == FORGE_PREC_MIXED) FORGE_TRY(x->mixws.ensure(eig_mixed_workspace_bytes(N, iu, B)));
     FORGE_TRY(c.bulk.ensure(4 * NN * sizeof(double2)));
@@ -177,8 +189,9 @@ int upload_state(forge_ctx* x, const double* Potential, const double* zFock) {
     return 0;
 }
 
-// eigen-solve of the batch of H already assembled in c.H for k in [k0, k0+nb)
-int eig_batch_run(forge_ctx* x, int64_t k0, int64_t nb, int* info) {
+// eigen-solve of the batch of H already assembled in c.H for k in [k0, k0+nb); the eigenpairs go to
+// the slots of those k, or to Xdst / wdst when given
+int eig_batch_run(forge_ctx* x, int64_t k0, int64_t nb, int* info, double2* Xdst = nullptr, double* wdst = nullptr) {
     Context& c = x->c;
     const int64_t N = c.N, iu = c.nUpper;
     EigArgs g{};
@@ -188,10 +201,10 @@ int eig_batch_run(forge_ctx* x, int64_t k0, int64_t nb, int* info) {
     g.A = c.H.as<double2>();
     g.lda = N;
     g.strideA = N * N;
-    g.X = c.X.as<double2>() + (size_t)k0 * N * iu;
+    g.X = Xdst ? Xdst : c.X.as<double2>() + (size_t)k0 * N * iu;
     g.ldx = N;
     g.strideX = N * iu;
-    g.w = x->w.as<double>() + (size_t)k0 * iu;
+    g.w = wdst ? wdst : x->w.as<double>() + (size_t)k0 * iu;
     g.ortol_rel = 1e-7;
     eig_bind_workspace(g, x->eigws.ptr);
     if (c.precision == FORGE_PREC_MIXED) {
@@ -235,6 +248,41 @@ int project_k(forge_ctx* x, int64_t k, int64_t K, const double2* ph, double2* ou
     return bulk_projector_fp64(c.stream, Xk, N, N, K, ph, out);
 }
 
+// project_k, with the average of Solve_C3 / GetFock_C3 at a C3-invariant k: the projector of k's
+// eigenvectors and of their two rotated copies, each with a third of the phases
+int project_k_c3(forge_ctx* x, int64_t k, int64_t K, const double2* ph, double2* out) {
+    if (!x->c3 || x->c3t.extra[k] < 0) return project_k(x, k, K, ph, out);
+    double2 ph3[4];
+    for (int t = 0; t < 4; ++t) ph3[t] = cscale(ph[t], 1.0 / 3.0);
+    const int64_t e = x->c3t.extra[k];
+    FORGE_TRY(project_k(x, k, K, ph3, out));
+    FORGE_TRY(project_k(x, e, K, ph3, out));
+    return project_k(x, e + 1, K, ph3, out);
+}
+
+// window states with the C3 average: a state at a C3-invariant k becomes itself and its two
+// rotated copies, each with a third of its weighted phases (GetFock_C3, HartreeFock.f90:650-876)
+void expand_c3_states(forge_ctx* x, std::vector<WinState>& st) {
+    if (!x->c3) return;
+    std::vector<WinState> out;
+    out.reserve(st.size());
+    for (const WinState& s0 : st) {
+        const int64_t e = x->c3t.extra[s0.k];
+        if (e < 0) {
+            out.push_back(s0);
+            continue;
+        }
+        WinState s = s0;
+        for (int t = 0; t < 4; ++t) s.wph[t] = cscale(s0.wph[t], 1.0 / 3.0);
+        out.push_back(s);
+        s.k = e;
+        out.push_back(s);
+        s.k = e + 1;
+        out.push_back(s);
+    }
+    st.swap(out);
+}
+
 // full Solve on the device: H(k), eigenpairs, and (with_projector) the bulk projector of bands
 // 1..nLower-1 (not divided by Nk), as Solve returns it
 int solve_device(forge_ctx* x, int* info, bool with_projector = true) {
@@ -251,6 +299,33 @@ int solve_device(forge_ctx* x, int* info, bool with_projector = true) {
     if (x->tcerr.ptr) FORGE_CUDA(cudaMemsetAsync(x->tcerr.ptr, 0, sizeof(int), c.stream));
     // local k range of this rank (all k unless forge_gpu_set_kshard narrowed it)
     const int64_t kb = x->k_begin, ke = (x->k_end > 0) ? x->k_end : Nk;
+    if (x->c3) {
+        if (kb != 0 || ke != Nk) {
+            set_error(FORGE_ERR_STATE, "the C3-reduced solve runs over the whole k grid (no k shard)");
+            return FORGE_ERR_STATE;
+        }
+        // Solve_C3 (HartreeFock.f90:189-216): the orbit representatives in batches, then the rotated
+        // eigenvectors and the copied bands of every k
+        const int64_t N_ = c.N, iu = c.nUpper, nr = (int64_t)x->c3t.reps.size();
+        for (int64_t r0 = 0; r0 < nr; r0 += B) {
+            const int64_t nb = (nr - r0 < B) ? nr - r0 : B;
+            for (int64_t b = 0; b < nb; ++b)
+                FORGE_TRY(launch_assemble(c, c.V.as<double>(), c.P.as<double2>(), x->c3t.reps[r0 + b], 1,
+                                          c.H.as<double2>() + (size_t)b * NN));
+            FORGE_TRY(eig_batch_run(x, r0, nb, info, x->c3_Xr.as<double2>() + (size_t)r0 * N_ * iu,
+                                    x->c3_wr.as<double>() + (size_t)r0 * iu));
+        }
+        FORGE_TRY(launch_c3_rotate(c.stream, x->c3_Xr.as<double2>(), x->c3_wr.as<double>(), N_, iu, x->c3t.nslots,
+                                   x->c3_tab.as<int64_t>(), x->c3_perm.as<int64_t>(), x->c3_phase.as<double2>(),
+                                   c.X.as<double2>(), x->w.as<double>()));
+        if (with_projector)
+            for (int64_t k = 0; k < Nk; ++k)
+                FORGE_TRY(project_k_c3(x, k, c.nLower - 1, &x->h_bph[k * 4], c.bulk.as<double2>()));
+        x->have_solve = true;
+        x->have_sort = false;
+        x->bulk_is_fused = !with_projector;
+        return 0;
+    }
     for (int64_t k0 = kb; k0 < ke; k0 += B) {
         const int64_t nb = (ke - k0 < B) ? ke - k0 : B;
         FORGE_TRY(launch_assemble(c, c.V.as<double>(), c.P.as<double2>(), k0, nb, c.H.as<double2>()));
@@ -300,11 +375,12 @@ int project_fused_once(forge_ctx* x) {
     if (x->tcerr.ptr) FORGE_CUDA(cudaMemsetAsync(x->tcerr.ptr, 0, sizeof(int), c.stream));
     const int64_t kb = x->k_begin, ke = (x->k_end > 0) ? x->k_end : Nk;
     for (int64_t k = kb; k < ke; ++k)
-        FORGE_TRY(project_k(x, k, c.nLower - 1 + fk[k], &x->h_bph[k * 4], x->Pn.as<double2>()));
+        FORGE_TRY(project_k_c3(x, k, c.nLower - 1 + fk[k], &x->h_bph[k * 4], x->Pn.as<double2>()));
     // partially occupied states of local k points (complex weight zdeg in reference mode)
     std::vector<WinState> part;
     for (int64_t q = nocc - npart; q < nocc; ++q)
         if (st[q].k >= kb && st[q].k < ke) part.push_back(st[q]);
+    expand_c3_states(x, part);
     if (!part.empty()) {
         // the partial states go to their own buffer: x->states keeps the sorted list (a second
         // formation of P_new reads it again)
@@ -651,7 +727,8 @@ int forge_gpu_finalize(forge_ctx* x) {
                       &c.dens_in, &c.V_old, &c.H, &c.X, &c.bands, &c.evals, &c.kvecs, &c.kphase, &c.bphase,
                       &c.sort_idx, &c.sort_e, &c.red, &c.scalars, &x->te, &x->Pn, &x->win, &x->eigws, &x->mixws,
                       &x->states, &x->sorted_e, &x->sorted_idx, &x->sc, &x->work, &x->y, &x->dens_new, &x->w,
-                      &x->projws, &x->tcerr, &x->diis_hist, &x->diis_rprev, &x->diis_part, &x->rrws, &x->pstates};
+                      &x->projws, &x->tcerr, &x->diis_hist, &x->diis_rprev, &x->diis_part, &x->rrws, &x->pstates,
+                      &x->c3_Xr, &x->c3_wr, &x->c3_tab, &x->c3_perm, &x->c3_phase};
     for (DevBuf* b : bufs) b->release();
     if (c.stream) cudaStreamDestroy(c.stream);
     delete x;
@@ -679,6 +756,59 @@ int forge_gpu_set_refinement(forge_ctx* x, int64_t width) {
         return FORGE_ERR_ARG;
     }
     x->rr_width = width;
+    return 0;
+}
+
+int forge_gpu_set_c3(forge_ctx* x, int64_t nenforceC3, const int64_t* nC3pairs, const int64_t* RotateLayers) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (nenforceC3 == 0) {
+        x->c3 = false;
+        x->have_solve = x->have_sort = false;
+        return 0;
+    }
+    if (nenforceC3 != 1 || !nC3pairs || !RotateLayers) {
+        set_error(FORGE_ERR_ARG, "set_c3: nenforceC3 must be 0 or 1, with nC3pairs and RotateLayers");
+        return FORGE_ERR_ARG;
+    }
+    if (c.s.fphase != 0) {
+        set_error(FORGE_ERR_ARG, "set_c3: the C3-reduced solve is implemented for fphase = 0");
+        return FORGE_ERR_ARG;
+    }
+    const int64_t N = c.N;
+    // nC3pairs (C3_RelatedPoints, Geometry.f90:1172-1223) must be a permutation of the sites
+    std::vector<char> seen(N, 0);
+    for (int64_t i = 0; i < N; ++i) {
+        const int64_t j = nC3pairs[i];
+        if (j < 1 || j > N || seen[j - 1]) {
+            set_error(FORGE_ERR_ARG, "set_c3: nC3pairs is not a permutation of 1..%lld (site %lld)", (long long)N,
+                      (long long)(i + 1));
+            return FORGE_ERR_ARG;
+        }
+        seen[j - 1] = 1;
+    }
+    C3Tables t;
+    FORGE_TRY(c3_build_tables(c.s.numk, N, c.s.nlayers, c.kcomp.data(), RotateLayers, t));
+    std::vector<int64_t> perm(3 * N);
+    for (int64_t i = 0; i < N; ++i) {
+        perm[i] = i;
+        perm[N + i] = nC3pairs[i] - 1;
+        perm[2 * N + i] = nC3pairs[nC3pairs[i] - 1] - 1;
+    }
+    FORGE_TRY(x->c3_tab.ensure(t.slot_tab.size() * sizeof(int64_t)));
+    FORGE_TRY(x->c3_perm.ensure(perm.size() * sizeof(int64_t)));
+    FORGE_TRY(x->c3_phase.ensure(t.phase.size() * sizeof(double2)));
+    FORGE_CUDA(cudaMemcpyAsync(x->c3_tab.ptr, t.slot_tab.data(), t.slot_tab.size() * sizeof(int64_t),
+                               cudaMemcpyHostToDevice, c.stream));
+    FORGE_CUDA(cudaMemcpyAsync(x->c3_perm.ptr, perm.data(), perm.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                               c.stream));
+    FORGE_CUDA(cudaMemcpyAsync(x->c3_phase.ptr, t.phase.data(), t.phase.size() * sizeof(double2),
+                               cudaMemcpyHostToDevice, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    x->c3t = std::move(t);
+    x->c3 = true;
+    x->eig_batch = 0;
+    x->have_solve = x->have_sort = false;
     return 0;
 }
 
@@ -1049,9 +1179,15 @@ int forge_gpu_get_fock(forge_ctx* x, double DegFactor, int64_t nOccStates, int64
         const double2 wgt = (q < nOccStates - nPartOccStates) ? make_double2(1.0, 0.0) : zdeg;
         for (int t = 0; t < 4; ++t) st[q].wph[t] = cmul(bph[k * 4 + t], wgt);
     }
-    FORGE_CUDA(cudaMemcpyAsync(x->states.ptr, st.data(), nOccStates * sizeof(WinState), cudaMemcpyHostToDevice,
-                               c.stream));
-    FORGE_TRY(get_fock_device(x, nOccStates));
+    if (nOccStates == 0) st.clear();
+    expand_c3_states(x, st);
+    const int64_t nst = (int64_t)st.size();
+    if (nst > 0) {
+        FORGE_TRY(x->states.ensure(nst * sizeof(WinState)));
+        FORGE_CUDA(cudaMemcpyAsync(x->states.ptr, st.data(), nst * sizeof(WinState), cudaMemcpyHostToDevice,
+                                   c.stream));
+    }
+    FORGE_TRY(get_fock_device(x, nst));
     if (zFock)
         FORGE_CUDA(cudaMemcpyAsync(zFock, x->Pn.ptr, 4 * (size_t)c.N * c.N * sizeof(double2), cudaMemcpyDeviceToHost,
                                    c.stream));

@@ -154,6 +154,20 @@ int launch_potential(Context& c, const double* dens, double* V);
 int launch_mix(Context& c, double step, double2* P, const double2* P_new, const double2* P_in, double* dens,
                const double* dens_in, double* out);
 
+// C3-reduced solve (c3.cu)
+struct C3Tables {
+    std::vector<int64_t> reps;      // 0-based k of the first point of each C3 orbit
+    int64_t nslots = 0;             // eigenvector slots: Nk, plus two per C3-invariant k
+    std::vector<int64_t> slot_tab;  // per slot: representative index, rotation (0 none, 1 nC3pairs, 2 twice)
+    std::vector<int64_t> extra;     // per k: its first extra slot (invariant k) or -1
+    std::vector<double2> phase;     // per slot: the N site phases of the rotation
+};
+bool c3_invariant(int64_t numk, int64_t k);
+int c3_build_tables(int64_t numk, int64_t N, int64_t nlayers, const int64_t* kcomp, const int64_t* RotateLayers,
+                    C3Tables& t);
+int launch_c3_rotate(cudaStream_t st, const double2* Xr, const double* wr, int64_t N, int64_t iu, int64_t nslots,
+                     const int64_t* slot_tab, const int64_t* perm, const double2* phase, double2* X, double* w);
+
 // device helpers shared across units
 __device__ double dev_ft(const forge_setup& s, double xi, double yi, double zi, double xj, double yj, double zj);
 __device__ double dev_fv(const forge_setup& s, double xi, double yi, double zi, double xj, double yj, double zj);

@@ -207,6 +207,15 @@ int forge_gpu_set_mixing(forge_ctx* ctx, int64_t mode, int64_t depth, double bet
  * against the FP64 H(k): Y = H X, G = X^H Y, S = X^H X, then G z = theta S z on the host. */
 int forge_gpu_set_refinement(forge_ctx* ctx, int64_t width);
 
+/* nenforceC3 (Setup.f90:27): 1 selects Solve_C3 / GetFock_C3 (HartreeFock.f90:131-398, 564-881) in
+ * every later solve and projector; 0 (the default) the full solve.  nC3pairs is the 1-based site map
+ * of C3_RelatedPoints (Geometry.f90:1172-1223, a permutation), RotateLayers the nlayers layer
+ * rotations (Setup.f90).  H(k) is solved only for the first k of each C3 orbit; the other two k get
+ * the representative's eigenvectors with rows permuted by nC3pairs and the corner sites phased, and
+ * at the three C3-invariant k the projectors are the average of the k's projector and its two
+ * rotated copies.  Needs numk divisible by 3 and fphase = 0 (FORGE_ERR_ARG otherwise), and no k shard. */
+int forge_gpu_set_c3(forge_ctx* ctx, int64_t nenforceC3, const int64_t* nC3pairs, const int64_t* RotateLayers);
+
 /* Selects FORGE_PREC_FP64 or FORGE_PREC_MIXED for subsequent solves. */
 int forge_gpu_set_precision(forge_ctx* ctx, int64_t precision);
 
