@@ -118,6 +118,8 @@ SIGNATURES = {
     "forge_host_write_fock": [_P, _P, C.c_char_p, _I],
     "forge_host_read_fock": [_P, _P, C.c_char_p, _I],
     "forge_gpu_set_c3": [_P, _I, _P, _P],
+    "forge_gpu_set_symmetry": [_P, _I, _I, _I, _P],
+    "forge_gpu_symmetrize": [_P, _P],
     "forge_host_sort_energies_2spins": [_I, _I, _P, _P, _P],
     "forge_host_fermi_2spins": [_P, _P, _P, _P, _P, _P, _P, _P],
 }
@@ -187,6 +189,9 @@ class Setup:
     fphase: int = 0
     numS: int = 1
     nenforceC3: int = 0
+    nenforceC2: int = 0
+    nenforceT: int = 0
+    nenforceC2T: int = 0
     EnergyTolerance: float = 0.0001
     StepAlternative: float = 1.0
     degfactor_mode: str = "reference"
@@ -327,6 +332,8 @@ class HartreeFock:
         self.lib = lib
         if setup.nenforceC3:
             self.set_c3(setup.nenforceC3)
+        if setup.nenforceT or setup.nenforceC2 or setup.nenforceC2T:
+            self.set_symmetry(setup.nenforceT, setup.nenforceC2, setup.nenforceC2T)
 
     def close(self):
         if getattr(self, "ctx", None):
@@ -361,6 +368,17 @@ class HartreeFock:
         pairs = _f(self.geometry.nC3pairs, np.int64)
         rl = np.ascontiguousarray(self.setup.RotateLayers, dtype=np.int64)
         _check(self.lib.forge_gpu_set_c3(self.ctx, nenforceC3, _ptr(pairs), _ptr(rl)))
+
+    def set_symmetry(self, nenforceT: int = 0, nenforceC2: int = 0, nenforceC2T: int = 0):
+        """Symmetry averages of Main.f90:513-534 on every new density matrix of the SCF loop."""
+        pairs = _f(self.geometry.nC2pairs, np.int64)
+        _check(self.lib.forge_gpu_set_symmetry(self.ctx, nenforceT, nenforceC2, nenforceC2T, _ptr(pairs)))
+
+    def Symmetrize(self, copy_out: bool = True):
+        """Main.f90:513-534 on the device P_new of GetFock (the switches of set_symmetry)."""
+        P = np.zeros(self._zfock_shape(), dtype=np.complex128, order="F") if copy_out else None
+        _check(self.lib.forge_gpu_symmetrize(self.ctx, _ptr(P)))
+        return P
 
     def set_mixing(self, mode: str = "oda", depth: int = 6, beta: float = 0.7):
         """SCF mixing: "oda" (the reference's OptimalStep) or "pulay" (Anderson / Pulay, `depth` steps)."""

@@ -111,6 +111,9 @@ struct forge_ctx {
     bool c3 = false;
     C3Tables c3t;
     DevBuf c3_Xr, c3_wr, c3_tab, c3_perm, c3_phase;
+    // symmetry switches applied to P_new in the fused iteration (forge_gpu_set_symmetry)
+    bool sym_T = false, sym_C2 = false, sym_C2T = false;
+    DevBuf c2_perm;
     bool have_solve = false, have_sort = false, have_pnew = false, have_state = false, bulk_is_fused = false;
     std::vector<int64_t> h_sorted_idx;
     std::vector<double2> h_bph;
@@ -403,6 +406,19 @@ int project_fused_once(forge_ctx* x) {
     }
     x->have_pnew = true;
     return 0;
+}
+
+// Main.f90:513-534 on P_new: time reversal, C2, C2T as switched on
+int symmetrize_pnew(forge_ctx* x) {
+    if (!(x->sym_T || x->sym_C2 || x->sym_C2T)) return 0;
+    Context& c = x->c;
+    if (!x->have_pnew) {
+        set_error(FORGE_ERR_STATE, "symmetrize needs a new density matrix (get_fock) first");
+        return FORGE_ERR_STATE;
+    }
+    FORGE_TRY(x->win.ensure(4 * (size_t)c.N * c.N * sizeof(double2)));
+    return launch_symmetrize(c.stream, x->Pn.as<double2>(), x->win.as<double2>(), x->c2_perm.as<int64_t>(), c.N,
+                             x->sym_T, x->sym_C2, x->sym_C2T);
 }
 
 // forget the mixing history (new state, new precision)
@@ -728,7 +744,7 @@ int forge_gpu_finalize(forge_ctx* x) {
                       &c.sort_idx, &c.sort_e, &c.red, &c.scalars, &x->te, &x->Pn, &x->win, &x->eigws, &x->mixws,
                       &x->states, &x->sorted_e, &x->sorted_idx, &x->sc, &x->work, &x->y, &x->dens_new, &x->w,
                       &x->projws, &x->tcerr, &x->diis_hist, &x->diis_rprev, &x->diis_part, &x->rrws, &x->pstates,
-                      &x->c3_Xr, &x->c3_wr, &x->c3_tab, &x->c3_perm, &x->c3_phase};
+                      &x->c3_Xr, &x->c3_wr, &x->c3_tab, &x->c3_perm, &x->c3_phase, &x->c2_perm};
     for (DevBuf* b : bufs) b->release();
     if (c.stream) cudaStreamDestroy(c.stream);
     delete x;
@@ -809,6 +825,56 @@ int forge_gpu_set_c3(forge_ctx* x, int64_t nenforceC3, const int64_t* nC3pairs, 
     x->c3 = true;
     x->eig_batch = 0;
     x->have_solve = x->have_sort = false;
+    return 0;
+}
+
+int forge_gpu_set_symmetry(forge_ctx* x, int64_t nenforceT, int64_t nenforceC2, int64_t nenforceC2T,
+                           const int64_t* nC2pairs) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    auto flag = [](int64_t v) { return v == 0 || v == 1; };
+    if (!flag(nenforceT) || !flag(nenforceC2) || !flag(nenforceC2T)) {
+        set_error(FORGE_ERR_ARG, "set_symmetry: the switches are 0 or 1");
+        return FORGE_ERR_ARG;
+    }
+    if (nenforceC2 || nenforceC2T) {
+        // nC2pairs (C2_RelatedPoints, Geometry.f90:1140-1167) must pair every site
+        const int64_t N = c.N;
+        if (!nC2pairs) {
+            set_error(FORGE_ERR_ARG, "set_symmetry: C2 / C2T need nC2pairs");
+            return FORGE_ERR_ARG;
+        }
+        std::vector<char> seen(N, 0);
+        std::vector<int64_t> perm(N);
+        for (int64_t i = 0; i < N; ++i) {
+            const int64_t j = nC2pairs[i];
+            if (j < 1 || j > N || seen[j - 1]) {
+                set_error(FORGE_ERR_ARG, "set_symmetry: nC2pairs is not a permutation of 1..%lld (site %lld)",
+                          (long long)N, (long long)(i + 1));
+                return FORGE_ERR_ARG;
+            }
+            seen[j - 1] = 1;
+            perm[i] = j - 1;
+        }
+        FORGE_TRY(x->c2_perm.ensure(N * sizeof(int64_t)));
+        FORGE_CUDA(cudaMemcpyAsync(x->c2_perm.ptr, perm.data(), N * sizeof(int64_t), cudaMemcpyHostToDevice,
+                                   c.stream));
+        FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    }
+    x->sym_T = nenforceT == 1;
+    x->sym_C2 = nenforceC2 == 1;
+    x->sym_C2T = nenforceC2T == 1;
+    return 0;
+}
+
+int forge_gpu_symmetrize(forge_ctx* x, double* zFock) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    FORGE_TRY(symmetrize_pnew(x));
+    if (zFock)
+        FORGE_CUDA(cudaMemcpyAsync(zFock, x->Pn.ptr, 4 * (size_t)c.N * c.N * sizeof(double2), cudaMemcpyDeviceToHost,
+                                   c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
     return 0;
 }
 
@@ -1369,6 +1435,7 @@ int forge_gpu_scf_iteration(forge_ctx* x, double* Energies, forge_iter_report* r
     FORGE_TRY(solve_device(x, &info, false));
     FORGE_TRY(sort_device(x, c.s.nfilling));
     FORGE_TRY(project_fused(x));
+    FORGE_TRY(symmetrize_pnew(x));
     FORGE_TRY(scf_density(c, x->Pn.as<double2>(), x->dens_new.as<double>()));
     FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(),
                                x->dens_new.as<double>(), x->y.as<double>(), x->work.as<double>(),

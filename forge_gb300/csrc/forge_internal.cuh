@@ -168,6 +168,10 @@ int c3_build_tables(int64_t numk, int64_t N, int64_t nlayers, const int64_t* kco
 int launch_c3_rotate(cudaStream_t st, const double2* Xr, const double* wr, int64_t N, int64_t iu, int64_t nslots,
                      const int64_t* slot_tab, const int64_t* perm, const double2* phase, double2* X, double* w);
 
+// symmetry switches of the SCF loop (symmetry.cu)
+int launch_symmetrize(cudaStream_t st, double2* P, double2* scratch, const int64_t* perm, int64_t N, bool T, bool C2,
+                      bool C2T);
+
 // device helpers shared across units
 __device__ double dev_ft(const forge_setup& s, double xi, double yi, double zi, double xj, double yj, double zj);
 __device__ double dev_fv(const forge_setup& s, double xi, double yi, double zi, double xj, double yj, double zj);

@@ -216,6 +216,17 @@ int forge_gpu_set_refinement(forge_ctx* ctx, int64_t width);
  * rotated copies.  Needs numk divisible by 3 and fphase = 0 (FORGE_ERR_ARG otherwise), and no k shard. */
 int forge_gpu_set_c3(forge_ctx* ctx, int64_t nenforceC3, const int64_t* nC3pairs, const int64_t* RotateLayers);
 
+/* nenforceT, nenforceC2, nenforceC2T (Setup.f90:28-30), each 0 (default) or 1: the symmetry
+ * averages of Main.f90:513-534 on every new density matrix of forge_gpu_scf_iteration (not on the
+ * initial guess), in the order T, C2, C2T.  nC2pairs (1-based, a permutation; C2_RelatedPoints,
+ * Geometry.f90:1140-1167) is read when C2 or C2T is on and may be NULL otherwise. */
+int forge_gpu_set_symmetry(forge_ctx* ctx, int64_t nenforceT, int64_t nenforceC2, int64_t nenforceC2T,
+                           const int64_t* nC2pairs);
+
+/* The same averages on the device P_new of forge_gpu_get_fock, for hosts that call the routines one
+ * by one; copies the result to zFock when it is not NULL. */
+int forge_gpu_symmetrize(forge_ctx* ctx, double* zFock);
+
 /* Selects FORGE_PREC_FP64 or FORGE_PREC_MIXED for subsequent solves. */
 int forge_gpu_set_precision(forge_ctx* ctx, int64_t precision);
 

@@ -46,7 +46,8 @@ class Setup:
     ``zdeg = cmplx(DegFactor, dp)`` (HartreeFock.f90:529) literally, i.e. the
     single-precision real part and an imaginary part equal to ``dp`` = 8;
     ``"corrected"`` uses the real weight DegFactor.  ``nenforceC3 = 1`` (Setup.f90:27) selects
-    Solve_C3 / GetFock_C3 in the SCF drivers.
+    Solve_C3 / GetFock_C3 in the SCF drivers; ``nenforceC2``, ``nenforceT``, ``nenforceC2T``
+    (Setup.f90:28-30) symmetrise every new density matrix of the SCF loop (``enforce_symmetries``).
     """
 
     ntheta: int = 5
@@ -68,6 +69,9 @@ class Setup:
     pressure: float = 1.0
     numS: int = 1
     nenforceC3: int = 0
+    nenforceC2: int = 0
+    nenforceT: int = 0
+    nenforceC2T: int = 0
     degfactor_mode: str = "reference"
 
     # derived (Setup.f90:10, 23-24, 58-69)
@@ -910,6 +914,29 @@ def get_fock_c3(s: Setup, g: Geometry, sorted_vecs, moms, nocc: int, npart: int,
     return out
 
 
+def enforce_symmetries(s: Setup, g: Geometry, P) -> np.ndarray:
+    """Main.f90:513-534, applied to the new zFock of each SCF iteration (not to the initial guess):
+    time reversal P <- Re P, then C2 P(m) <- (P(m) + conj(P(m)(p, p))^T)/2, then C2T
+    P(m) <- (P(m) + P(m)(p, p)^T)/2 for every cell m, p = nC2pairs.  The right-hand sides are
+    evaluated before the assignment, as in the Fortran array expressions."""
+    if not (s.nenforceT or s.nenforceC2 or s.nenforceC2T):
+        return P
+    P = np.array(P, dtype=np.complex128)
+    if s.nenforceT == 1:
+        P = P.real.astype(np.complex128)
+    if s.nenforceC2 == 1 or s.nenforceC2T == 1:
+        if np.any(g.c2pairs < 1):
+            raise ValueError("nC2pairs does not pair every site (C2_RelatedPoints reported a mismatch)")
+        p0 = g.c2pairs - 1
+    if s.nenforceC2 == 1:
+        for m in range(P.shape[0]):
+            P[m] = 0.5 * (P[m] + np.conj(P[m][np.ix_(p0, p0)].T))
+    if s.nenforceC2T == 1:
+        for m in range(P.shape[0]):
+            P[m] = 0.5 * (P[m] + P[m][np.ix_(p0, p0)].T)
+    return P
+
+
 def solve_any(s: Setup, g: Geometry, T: PairTables, potential, P):
     """Solve or Solve_C3 by nenforceC3 (Main.f90:244-250, 375-381)."""
     return solve_c3(s, g, T, potential, P) if s.nenforceC3 == 1 else solve(s, g, T, potential, P)
@@ -1024,7 +1051,7 @@ def hf_residual(s: Setup, T: PairTables, V_new, V_old, P_new, P_old) -> float:
 
 
 # ---------------------------------------------------------------------------
-# SCF driver (Main.f90:236-679, numS=1, no symmetry enforcement)
+# SCF driver (Main.f90:236-679, numS=1; symmetry switches of Main.f90:513-534 by the Setup flags)
 # ---------------------------------------------------------------------------
 @dataclasses.dataclass
 class IterationLog:
@@ -1139,7 +1166,7 @@ def run_scf(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTables] = No
         se, _, moms, sv, _, _ = sort_energies_1spin(s, g, sol["bands"], sol["evecs"])
         nF, EF, nocc, npart, degf = fermi_level(s, se)
         Pw = get_fock_any(s, g, sv, moms, nocc, npart, degf)
-        P_new = (Pw + sol["bulk"]) / complex(float(s.Nk), 0.0)
+        P_new = enforce_symmetries(s, g, (Pw + sol["bulk"]) / complex(float(s.Nk), 0.0))
         E_in, Etot_in = E, Etot
         dens_new = np.real(np.diagonal(P_new[0])).copy()
         if mixer is not None:
@@ -1299,7 +1326,7 @@ def _density_2spins(P) -> np.ndarray:
 def run_scf_2spins(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTables] = None, LR=None,
                    P_init=None, itmax: Optional[int] = None, residual_tol: Optional[float] = None,
                    keep_history: bool = False):
-    """Main.f90:236-679 for numS=2 with ODA mixing and no symmetry enforcement.
+    """Main.f90:236-679 for numS=2 with ODA mixing (symmetry switches as in run_scf).
 
     Per iteration: both spins are solved with their own potential and density matrix, sorted, merged
     by ``sort_energies_2spins``, occupied by ``fermi_level_2spins`` (one Fermi level and DegFactor,
@@ -1342,8 +1369,9 @@ def run_scf_2spins(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTable
             movs.append((moms, sv))
         me, ml = sort_energies_2spins(s.numk, s.numb, W, ses[0], ses[1])
         nF, EF, nocc, npart, degf = fermi_level_2spins(s, me, ml)
-        P_new = np.stack([(get_fock_any(s, g, movs[sp][1], movs[sp][0], nocc[sp], npart[sp], degf)
-                           + sols[sp]["bulk"]) / complex(float(s.Nk), 0.0) for sp in range(2)])
+        P_new = np.stack([enforce_symmetries(s, g, (get_fock_any(s, g, movs[sp][1], movs[sp][0], nocc[sp], npart[sp],
+                                                                  degf) + sols[sp]["bulk"]) / complex(float(s.Nk), 0.0))
+                          for sp in range(2)])
         E_in, Etot_in = E, Etot
         dens_new = _density_2spins(P_new)
         step, E, t1, t2 = optimal_step(s, T, LR, P_new, P_in, dens_new, dens_in, E_in,
