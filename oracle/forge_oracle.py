@@ -47,7 +47,8 @@ class Setup:
     single-precision real part and an imaginary part equal to ``dp`` = 8;
     ``"corrected"`` uses the real weight DegFactor.  ``nenforceC3 = 1`` (Setup.f90:27) selects
     Solve_C3 / GetFock_C3 in the SCF drivers; ``nenforceC2``, ``nenforceT``, ``nenforceC2T``
-    (Setup.f90:28-30) symmetrise every new density matrix of the SCF loop (``enforce_symmetries``).
+    (Setup.f90:28-30) symmetrise every new density matrix of the SCF loop (``enforce_symmetries``);
+    ``nenforceValley`` (Setup.f90:31) averages the window part with its valley transform (``window_fock``).
     """
 
     ntheta: int = 5
@@ -72,6 +73,7 @@ class Setup:
     nenforceC2: int = 0
     nenforceT: int = 0
     nenforceC2T: int = 0
+    nenforceValley: int = 0
     degfactor_mode: str = "reference"
 
     # derived (Setup.f90:10, 23-24, 58-69)
@@ -937,6 +939,100 @@ def enforce_symmetries(s: Setup, g: Geometry, P) -> np.ndarray:
     return P
 
 
+# ---------------------------------------------------------------------------
+# Valley projection (nenforceValley = 1; Main.f90:470-500, TightBinding.f90:60-270,
+# LapackRoutines.f90:241-267, 865-893)
+# ---------------------------------------------------------------------------
+def rot_matrix(s: Setup) -> np.ndarray:
+    """RotMatrix = reshape([c, -s, s, c], [2, 2]) with c, s of half the twist angle (Main.f90:133),
+    as a [row, col] array."""
+    m = s.ntheta
+    cs = 1.0 - 1.0 / (2.0 * (3.0 * m ** 2 + 3.0 * m + 1.0))
+    th = 0.5 * math.acos(cs)
+    return np.array([[math.cos(th), math.sin(th)], [-math.sin(th), math.cos(th)]])
+
+
+def ftvalley(dx, dy, Rm) -> np.ndarray:
+    """ftvalley (TightBinding.f90:235-270) of the separations (dx, dy) = r_i - r_j (arrays): i
+    sign(cos 3 phi)/sqrt(27) for 0.2 < |r_i - r_j| < 1.2, phi the angle of RotMatrix (r_i - r_j), and 0
+    otherwise."""
+    dx = np.asarray(dx, dtype=np.float64)
+    dy = np.asarray(dy, dtype=np.float64)
+    rij = np.sqrt(dx ** 2 + dy ** 2)
+    x = Rm[0, 0] * dx + Rm[0, 1] * dy
+    y = Rm[1, 0] * dx + Rm[1, 1] * dy
+    with np.errstate(divide="ignore", invalid="ignore"):
+        at = np.arctan(y / x)
+    phi = np.where(x > 0, at, np.where((x < 0) & (y > 0), at + PI, -PI + at))
+    phi = np.where(x == 0, np.where(y > 0, PI / 2.0, -PI / 2.0), phi)
+    val = 1j * np.copysign(1.0, np.cos(3.0 * phi)) / math.sqrt(27.0)
+    return np.where((rij < 1.2) & (rij > 0.2), val, 0.0 + 0.0j)
+
+
+def valley_phase(s: Setup, g: Geometry, vk) -> np.ndarray:
+    """ValleyPhase (TightBinding.f90:60-157), fphase = 0: the valley operator at k, nonzero only between
+    sites of the same sublattice block of a layer; each pair adds its term in the home cell and in
+    the neighbour cells R_c (r_j - R_c with exp(-i k.R_c), r_i - R_c with exp(+i k.R_c)), with
+    RotMatrix^T for layers rotated by -1 and RotMatrix for layers rotated by +1."""
+    if s.fphase != 0:
+        raise ValueError("the valley operator is restated for fphase = 0")
+    N = s.ndim
+    per = N // s.nlayers
+    R = rot_matrix(s)
+    X = g.coords
+    V = np.zeros((N, N), dtype=np.complex128)
+    for l in range(s.nlayers):
+        rl = int(s.RotateLayers[l])
+        if rl not in (-1, 1):
+            continue
+        Rm = R.T if rl == -1 else R
+        for lo, hi in ((per * l, per * l + per // 2), (per * l + per // 2, per * (l + 1))):
+            xi, yi = X[lo:hi, 0][:, None], X[lo:hi, 1][:, None]
+            xj, yj = X[lo:hi, 0][None, :], X[lo:hi, 1][None, :]
+            blk = ftvalley(xi - xj, yi - yj, Rm)
+            for c in range(1, len(g.ucell1)):
+                n1, n2 = float(g.ucell1[c]), float(g.ucell2[c])
+                sx, sy = n1 * g.t1[0] + n2 * g.t2[0], n1 * g.t1[1] + n2 * g.t2[1]
+                kr = float(vk[0] * sx + vk[1] * sy)
+                blk = blk + ftvalley(xi - ((xj - n1 * g.t1[0]) - n2 * g.t2[0]),
+                                     yi - ((yj - n1 * g.t1[1]) - n2 * g.t2[1]), Rm) * np.exp(complex(0.0, -kr))
+                blk = blk + ftvalley(((xi - n1 * g.t1[0]) - n2 * g.t2[0]) - xj,
+                                     ((yi - n1 * g.t1[1]) - n2 * g.t2[1]) - yj, Rm) * np.exp(complex(0.0, kr))
+            V[lo:hi, lo:hi] += blk
+    return V
+
+
+def unitarize(A: np.ndarray) -> np.ndarray:
+    """z_unitarize (LapackRoutines.f90:865-893): U sign(Lambda) U^H of the Hermitian A = U Lambda U^H
+    (sign(1, 0) = +1)."""
+    w, U = np.linalg.eigh(A)
+    return (U * np.copysign(1.0, w)[None, :]) @ U.conj().T
+
+
+def valley_transform(s: Setup, g: Geometry, evecs: np.ndarray) -> np.ndarray:
+    """ValleyTransform (TightBinding.f90:162-208): at every k the window eigenvectors X (N x numb)
+    become X unitarize(X^H V(k) X), V(k) = valley_phase."""
+    out = np.empty_like(evecs)
+    for ic in range(s.Nk):
+        a, b = (int(x) for x in g.kcomp[ic])
+        X = evecs[:, :, ic]
+        Vp = X.conj().T @ (valley_phase(s, g, g.kvals[a, b]) @ X)
+        out[:, :, ic] = X @ unitarize(Vp)
+    return out
+
+
+def window_fock(s: Setup, g: Geometry, sol: dict, sv, moms, nocc: int, npart: int, degf: float) -> np.ndarray:
+    """The window part of the new zFock (before + zFockBulk, / Nk): GetFock (or GetFock_C3), or with
+    nenforceValley = 1 the average of GetFock of the sorted eigenvectors and of their valley-transformed
+    copies (Main.f90:470-500: zFock = .5 (GetFock + GetFock after ValleyTransform) + zFockBulk)."""
+    Pw = get_fock_any(s, g, sv, moms, nocc, npart, degf)
+    if s.nenforceValley != 1:
+        return Pw
+    ev = valley_transform(s, g, sol["evecs"])
+    _, _, moms2, sv2, _, _ = sort_energies_1spin(s, g, sol["bands"], ev)
+    return 0.5 * (Pw + get_fock_any(s, g, sv2, moms2, nocc, npart, degf))
+
+
 def solve_any(s: Setup, g: Geometry, T: PairTables, potential, P):
     """Solve or Solve_C3 by nenforceC3 (Main.f90:244-250, 375-381)."""
     return solve_c3(s, g, T, potential, P) if s.nenforceC3 == 1 else solve(s, g, T, potential, P)
@@ -1165,7 +1261,7 @@ def run_scf(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTables] = No
         sol = solve_any(s, g, T, V, P)
         se, _, moms, sv, _, _ = sort_energies_1spin(s, g, sol["bands"], sol["evecs"])
         nF, EF, nocc, npart, degf = fermi_level(s, se)
-        Pw = get_fock_any(s, g, sv, moms, nocc, npart, degf)
+        Pw = window_fock(s, g, sol, sv, moms, nocc, npart, degf)
         P_new = enforce_symmetries(s, g, (Pw + sol["bulk"]) / complex(float(s.Nk), 0.0))
         E_in, Etot_in = E, Etot
         dens_new = np.real(np.diagonal(P_new[0])).copy()
@@ -1369,8 +1465,9 @@ def run_scf_2spins(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTable
             movs.append((moms, sv))
         me, ml = sort_energies_2spins(s.numk, s.numb, W, ses[0], ses[1])
         nF, EF, nocc, npart, degf = fermi_level_2spins(s, me, ml)
-        P_new = np.stack([enforce_symmetries(s, g, (get_fock_any(s, g, movs[sp][1], movs[sp][0], nocc[sp], npart[sp],
-                                                                  degf) + sols[sp]["bulk"]) / complex(float(s.Nk), 0.0))
+        P_new = np.stack([enforce_symmetries(s, g, (window_fock(s, g, sols[sp], movs[sp][1], movs[sp][0], nocc[sp],
+                                                                 npart[sp], degf) + sols[sp]["bulk"])
+                                             / complex(float(s.Nk), 0.0))
                           for sp in range(2)])
         E_in, Etot_in = E, Etot
         dens_new = _density_2spins(P_new)
