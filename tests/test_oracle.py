@@ -161,3 +161,20 @@ def test_oracle_pulay_mixing_reaches_the_optimalstep_fixed_point():
     assert len(pul["logs"]) < len(oda["logs"])
     assert np.max(np.abs(pul["P"] - oda["P"])) <= 1e-9
     assert abs(pul["Etot"] - oda["Etot"]) / so.ndim <= 1e-9
+
+
+def test_variant_fixtures_reproduce():
+    """Regression pins of the switches outside the configured path (C3, symmetry averages, valley
+    projection, numS = 2) on the m = 1 cell."""
+    import importlib.util
+    path = os.path.join(GOLDEN, "oracle_variants_m1_k3.npz")
+    if not os.path.exists(path):
+        pytest.skip("golden fixture missing")
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    gd = np.load(path)
+    for name, r in mg.variant_runs():
+        assert np.max(np.abs(np.array([l.E_in for l in r["logs"]]) - gd[name + "_E_in"])) < 1e-9, name
+        assert np.max(np.abs(np.array([l.step for l in r["logs"]]) - gd[name + "_step"])) < 1e-9, name
+        assert np.max(np.abs(r["P"] - gd[name + "_P"])) < 1e-10, name
