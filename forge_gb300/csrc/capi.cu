@@ -630,6 +630,11 @@ int forge_gpu_init(const forge_setup* s, const double* Coords, const int64_t* nU
         set_error(FORGE_ERR_ARG, "numS=%lld is not supported (only numS=1)", (long long)s->numS);
         return FORGE_ERR_ARG;
     }
+    if (s->fphase != 0) {
+        // the projectors apply no site phase exp(i vk.r fphase) (HartreeFock.f90:453, 514)
+        set_error(FORGE_ERR_ARG, "fphase=%lld is not supported (only fphase=0)", (long long)s->fphase);
+        return FORGE_ERR_ARG;
+    }
     if (s->numNeighborCells != 4) {
         set_error(FORGE_ERR_ARG, "numNeighborCells=%lld is not supported (numI=1 gives 4)",
                   (long long)s->numNeighborCells);

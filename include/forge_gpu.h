@@ -55,7 +55,7 @@ typedef struct forge_setup {
     int64_t numI;             /* Setup.f90:19 (only 1 is supported: 4 neighbour cells) */
     int64_t numC;             /* Setup.f90:20 */
     int64_t nscreen;          /* Setup.f90:21 */
-    int64_t fphase;           /* Setup.f90:25 */
+    int64_t fphase;           /* Setup.f90:25 (only 0: the projectors apply no site phase) */
     int64_t ndim;             /* Setup.f90:10 */
     int64_t numb;             /* Setup.f90:23 */
     int64_t nLower, nUpper;   /* Setup.f90:67-68 */

@@ -205,3 +205,20 @@ def test_host_fermi_2spins_matches_oracle(lib, nfilling, split):
     assert np.array_equal(r["SortedEnergies_2Spins"][:, 0], e)
     assert (r["nFermiLevel"], r["FermiEnergy"], r["nOccStates"], r["nPartOccStates"]) == (nF, EF, nocc, npart)
     assert r["DegFactor"] == deg
+
+
+def test_init_rejects_unsupported_setups_before_touching_the_device(lib):
+    """forge_gpu_init checks its arguments before any CUDA call: numS = 2 (one context per spin),
+    fphase = 1 (the projectors apply no site phase) and numI > 1 are FORGE_ERR_ARG."""
+    import ctypes as C
+    import forge_gb300 as fg
+    g = fg.build_geometry(fg.Setup(ntheta=1, numk=3))
+    keep = [np.asfortranarray(a) for a in (g.Coords, g.nUnitCell_1, g.nUnitCell_2, g.tn, g.MomentaValues,
+                                          g.nMomentaComponents)]
+    for kw in (dict(numS=2), dict(fphase=1)):
+        s = fg.Setup(ntheta=1, numk=3, **kw).to_struct()
+        ctx = C.c_void_p()
+        rc = lib.forge_gpu_init(C.byref(s), *[a.ctypes.data_as(C.c_void_p) for a in keep], C.byref(ctx))
+        assert rc == -1          # FORGE_ERR_ARG
+        assert not ctx.value
+        assert lib.forge_gpu_last_error()
