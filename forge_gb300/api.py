@@ -119,6 +119,7 @@ SIGNATURES = {
     "forge_host_read_fock": [_P, _P, C.c_char_p, _I],
     "forge_gpu_set_c3": [_P, _I, _P, _P],
     "forge_gpu_set_symmetry": [_P, _I, _I, _I, _P],
+    "forge_gpu_set_valley": [_P, _I, _P],
     "forge_gpu_symmetrize": [_P, _P],
     "forge_host_sort_energies_2spins": [_I, _I, _P, _P, _P],
     "forge_host_fermi_2spins": [_P, _P, _P, _P, _P, _P, _P, _P],
@@ -192,6 +193,7 @@ class Setup:
     nenforceC2: int = 0
     nenforceT: int = 0
     nenforceC2T: int = 0
+    nenforceValley: int = 0
     EnergyTolerance: float = 0.0001
     StepAlternative: float = 1.0
     degfactor_mode: str = "reference"
@@ -334,6 +336,8 @@ class HartreeFock:
             self.set_c3(setup.nenforceC3)
         if setup.nenforceT or setup.nenforceC2 or setup.nenforceC2T:
             self.set_symmetry(setup.nenforceT, setup.nenforceC2, setup.nenforceC2T)
+        if setup.nenforceValley:
+            self.set_valley(setup.nenforceValley)
 
     def close(self):
         if getattr(self, "ctx", None):
@@ -373,6 +377,11 @@ class HartreeFock:
         """Symmetry averages of Main.f90:513-534 on every new density matrix of the SCF loop."""
         pairs = _f(self.geometry.nC2pairs, np.int64)
         _check(self.lib.forge_gpu_set_symmetry(self.ctx, nenforceT, nenforceC2, nenforceC2T, _ptr(pairs)))
+
+    def set_valley(self, nenforceValley: int = 1):
+        """nenforceValley (Setup.f90:31): the valley average of Main.f90:470-500 on every new window."""
+        rl = np.ascontiguousarray(self.setup.RotateLayers, dtype=np.int64)
+        _check(self.lib.forge_gpu_set_valley(self.ctx, nenforceValley, _ptr(rl)))
 
     def Symmetrize(self, copy_out: bool = True):
         """Main.f90:513-534 on the device P_new of GetFock (the switches of set_symmetry)."""

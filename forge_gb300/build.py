@@ -26,6 +26,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path
 EXTRA = {
     "tables.cu": ["--fmad=false"],
     "capi.cu": ["-Xcompiler", "-ffp-contract=off"],
+    "valley.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
 
 

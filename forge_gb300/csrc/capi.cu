@@ -114,6 +114,9 @@ struct forge_ctx {
     // symmetry switches applied to P_new in the fused iteration (forge_gpu_set_symmetry)
     bool sym_T = false, sym_C2 = false, sym_C2T = false;
     DevBuf c2_perm;
+    // valley projection (forge_gpu_set_valley): V(k) terms, per-k phases, and the transform buffers
+    bool valley = false;
+    DevBuf v_rowp, v_col, v_coef, v_code, v_ph, v_W, v_G, v_S, v_Xv, v_st;
     bool have_solve = false, have_sort = false, have_pnew = false, have_state = false, bulk_is_fused = false;
     std::vector<int64_t> h_sorted_idx;
     std::vector<double2> h_bph;
@@ -406,6 +409,122 @@ int project_fused_once(forge_ctx* x) {
     }
     x->have_pnew = true;
     return 0;
+}
+
+// ValleyTransform (TightBinding.f90:162-208) of every k's window: Xv = X_win sign(X_win^H V(k) X_win)
+int valley_transform_device(forge_ctx* x) {
+    Context& c = x->c;
+    const int64_t N = c.N, iu = c.nUpper, c0 = c.nLower - 1, nb = c.numb, Nk = c.Nk;
+    FORGE_TRY(x->v_W.ensure((size_t)Nk * N * nb * sizeof(double2)));
+    FORGE_TRY(x->v_Xv.ensure((size_t)Nk * N * nb * sizeof(double2)));
+    FORGE_TRY(x->v_G.ensure((size_t)Nk * nb * nb * sizeof(double2)));
+    FORGE_TRY(x->v_S.ensure((size_t)Nk * nb * nb * sizeof(double2)));
+    FORGE_TRY(launch_valley_gram(c.stream, c.X.as<double2>(), N, iu, c0, nb, Nk, x->v_rowp.as<int64_t>(),
+                                 x->v_col.as<int64_t>(), x->v_coef.as<double>(), x->v_code.as<int>(),
+                                 x->v_ph.as<double2>(), x->v_W.as<double2>(), x->v_G.as<double2>()));
+    const size_t nn = (size_t)nb * nb;
+    std::vector<double2> G(Nk * nn), S(Nk * nn), I(nn, make_double2(0.0, 0.0)), U(nn), Gh(nn);
+    std::vector<double> th(nb);
+    for (int64_t a = 0; a < nb; ++a) I[a + a * nb] = make_double2(1.0, 0.0);
+    FORGE_CUDA(cudaMemcpyAsync(G.data(), x->v_G.ptr, G.size() * sizeof(double2), cudaMemcpyDeviceToHost, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    for (int64_t k = 0; k < Nk; ++k) {
+        // unitarize (LapackRoutines.f90:865-893): S = U sign(theta) U^H of the Hermitian part of G
+        const double2* g = G.data() + k * nn;
+        for (int64_t a = 0; a < nb; ++a)
+            for (int64_t b = 0; b < nb; ++b)
+                Gh[a + b * nb] = cscale(cadd(g[a + b * nb], cconj(g[b + a * nb])), 0.5);
+        if (rr_small((int)nb, Gh.data(), I.data(), th.data(), U.data())) {
+            set_error(FORGE_ERR_CUDA, "valley projection: the %lldx%lld eigen-problem failed", (long long)nb,
+                      (long long)nb);
+            return FORGE_ERR_CUDA;
+        }
+        double2* sk = S.data() + k * nn;
+        for (int64_t a = 0; a < nb; ++a)
+            for (int64_t b = 0; b < nb; ++b) {
+                double2 acc = make_double2(0.0, 0.0);
+                for (int64_t q = 0; q < nb; ++q)
+                    acc = cadd(acc, cscale(cmul(U[a + q * nb], cconj(U[b + q * nb])), std::copysign(1.0, th[q])));
+                sk[a + b * nb] = acc;
+            }
+    }
+    FORGE_CUDA(cudaMemcpyAsync(x->v_S.ptr, S.data(), S.size() * sizeof(double2), cudaMemcpyHostToDevice, c.stream));
+    FORGE_TRY(launch_valley_rotate(c.stream, c.X.as<double2>(), N, iu, c0, nb, Nk, x->v_S.as<double2>(),
+                                   x->v_Xv.as<double2>()));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+// Main.f90:470-500: Pn += (GetFock over the window states + GetFock over their valley transforms) / 2;
+// st holds every occupied window state with its weighted phases
+int valley_window(forge_ctx* x, const std::vector<WinState>& st) {
+    Context& c = x->c;
+    if (st.empty()) return 0;
+    FORGE_TRY(valley_transform_device(x));
+    const int64_t n = (int64_t)st.size(), c0 = c.nLower - 1;
+    std::vector<WinState> h(st), v(st);
+    for (int64_t q = 0; q < n; ++q) {
+        for (int t = 0; t < 4; ++t) h[q].wph[t] = v[q].wph[t] = cscale(st[q].wph[t], 0.5);
+        v[q].col = st[q].col - c0;
+    }
+    FORGE_TRY(x->pstates.ensure(n * sizeof(WinState)));
+    FORGE_TRY(x->v_st.ensure(n * sizeof(WinState)));
+    FORGE_CUDA(cudaMemcpyAsync(x->pstates.ptr, h.data(), n * sizeof(WinState), cudaMemcpyHostToDevice, c.stream));
+    FORGE_CUDA(cudaMemcpyAsync(x->v_st.ptr, v.data(), n * sizeof(WinState), cudaMemcpyHostToDevice, c.stream));
+    FORGE_TRY(window_projector_fp64(c.stream, x->pstates.as<WinState>(), n, c.X.as<double2>(), c.N, c.N * c.nUpper, c.N,
+                                    x->Pn.as<double2>()));
+    FORGE_TRY(window_projector_fp64(c.stream, x->v_st.as<WinState>(), n, x->v_Xv.as<double2>(), c.N, c.N * c.numb,
+                                    c.N, x->Pn.as<double2>()));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+// P_new with the valley average, for the fused iteration: the bulk bands of every k, then the
+// averaged window of Main.f90:470-500, divided by Nk
+int project_valley_once(forge_ctx* x) {
+    Context& c = x->c;
+    const int64_t N = c.N, Nk = c.Nk;
+    const size_t NN = (size_t)N * N;
+    if (x->k_begin != 0 || (x->k_end > 0 && x->k_end != Nk)) {
+        set_error(FORGE_ERR_STATE, "the valley projection runs over the whole k grid (no k shard)");
+        return FORGE_ERR_STATE;
+    }
+    ScfScalars h;
+    FORGE_TRY(read_scalars(x, &h));
+    const int64_t nocc = h.nOcc;
+    std::vector<WinState> st(nocc > 0 ? nocc : 0);
+    if (nocc > 0)
+        FORGE_CUDA(cudaMemcpyAsync(st.data(), x->states.ptr, nocc * sizeof(WinState), cudaMemcpyDeviceToHost,
+                                   c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    FORGE_TRY(x->Pn.ensure(4 * NN * sizeof(double2)));
+    FORGE_CUDA(cudaMemsetAsync(x->Pn.ptr, 0, 4 * NN * sizeof(double2), c.stream));
+    if (x->tcerr.ptr) FORGE_CUDA(cudaMemsetAsync(x->tcerr.ptr, 0, sizeof(int), c.stream));
+    for (int64_t k = 0; k < Nk; ++k)
+        FORGE_TRY(project_k(x, k, c.nLower - 1, &x->h_bph[k * 4], x->Pn.as<double2>()));
+    FORGE_TRY(valley_window(x, st));
+    FORGE_CUDA(cudaMemsetAsync(c.bulk.ptr, 0, 4 * NN * sizeof(double2), c.stream));
+    FORGE_TRY(scf_combine(c, x->Pn.as<double2>(), c.bulk.as<double2>()));
+    if (x->tcerr.ptr) {
+        int herr = 0;
+        FORGE_CUDA(cudaMemcpyAsync(&herr, x->tcerr.ptr, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        FORGE_CUDA(cudaStreamSynchronize(c.stream));
+        if (herr) {
+            set_error(FORGE_ERR_TIMEOUT, "tcgen05 projector: a bounded mbarrier wait gave up");
+            return FORGE_ERR_TIMEOUT;
+        }
+    }
+    x->have_pnew = true;
+    return 0;
+}
+
+int project_valley(forge_ctx* x) {
+    int rc = project_valley_once(x);
+    if (rc == FORGE_ERR_TIMEOUT) {
+        std::fprintf(stderr, "forge: %s; forming P_new again\n", forge_gpu_last_error());
+        rc = project_valley_once(x);
+    }
+    return rc;
 }
 
 // Main.f90:513-534 on P_new: time reversal, C2, C2T as switched on
@@ -749,7 +868,9 @@ int forge_gpu_finalize(forge_ctx* x) {
                       &c.sort_idx, &c.sort_e, &c.red, &c.scalars, &x->te, &x->Pn, &x->win, &x->eigws, &x->mixws,
                       &x->states, &x->sorted_e, &x->sorted_idx, &x->sc, &x->work, &x->y, &x->dens_new, &x->w,
                       &x->projws, &x->tcerr, &x->diis_hist, &x->diis_rprev, &x->diis_part, &x->rrws, &x->pstates,
-                      &x->c3_Xr, &x->c3_wr, &x->c3_tab, &x->c3_perm, &x->c3_phase, &x->c2_perm};
+                      &x->c3_Xr, &x->c3_wr, &x->c3_tab, &x->c3_perm, &x->c3_phase, &x->c2_perm,
+                      &x->v_rowp, &x->v_col, &x->v_coef, &x->v_code, &x->v_ph, &x->v_W, &x->v_G, &x->v_S,
+                      &x->v_Xv, &x->v_st};
     for (DevBuf* b : bufs) b->release();
     if (c.stream) cudaStreamDestroy(c.stream);
     delete x;
@@ -796,6 +917,10 @@ int forge_gpu_set_c3(forge_ctx* x, int64_t nenforceC3, const int64_t* nC3pairs, 
         set_error(FORGE_ERR_ARG, "set_c3: the C3-reduced solve is implemented for fphase = 0");
         return FORGE_ERR_ARG;
     }
+    if (x->valley) {
+        set_error(FORGE_ERR_ARG, "set_c3: the C3-reduced solve is not combined with the valley projection");
+        return FORGE_ERR_ARG;
+    }
     const int64_t N = c.N;
     // nC3pairs (C3_RelatedPoints, Geometry.f90:1172-1223) must be a permutation of the sites
     std::vector<char> seen(N, 0);
@@ -830,6 +955,45 @@ int forge_gpu_set_c3(forge_ctx* x, int64_t nenforceC3, const int64_t* nC3pairs, 
     x->c3 = true;
     x->eig_batch = 0;
     x->have_solve = x->have_sort = false;
+    return 0;
+}
+
+int forge_gpu_set_valley(forge_ctx* x, int64_t nenforceValley, const int64_t* RotateLayers) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (nenforceValley == 0) {
+        x->valley = false;
+        return 0;
+    }
+    if (nenforceValley != 1 || !RotateLayers) {
+        set_error(FORGE_ERR_ARG, "set_valley: nenforceValley must be 0 or 1, with RotateLayers");
+        return FORGE_ERR_ARG;
+    }
+    if (x->c3) {
+        set_error(FORGE_ERR_ARG, "set_valley: the valley projection is not combined with the C3-reduced solve");
+        return FORGE_ERR_ARG;
+    }
+    ValleyTerms t;
+    FORGE_TRY(valley_build_terms(c, RotateLayers, t));
+    std::vector<double2> ph;
+    valley_phases(c, ph);
+    const size_t nnz = t.col.size();
+    FORGE_TRY(x->v_rowp.ensure(t.rowp.size() * sizeof(int64_t)));
+    FORGE_TRY(x->v_col.ensure((nnz ? nnz : 1) * sizeof(int64_t)));
+    FORGE_TRY(x->v_coef.ensure((nnz ? nnz : 1) * sizeof(double)));
+    FORGE_TRY(x->v_code.ensure((nnz ? nnz : 1) * sizeof(int)));
+    FORGE_TRY(x->v_ph.ensure(ph.size() * sizeof(double2)));
+    FORGE_CUDA(cudaMemcpyAsync(x->v_rowp.ptr, t.rowp.data(), t.rowp.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                               c.stream));
+    if (nnz) {
+        FORGE_CUDA(cudaMemcpyAsync(x->v_col.ptr, t.col.data(), nnz * sizeof(int64_t), cudaMemcpyHostToDevice, c.stream));
+        FORGE_CUDA(cudaMemcpyAsync(x->v_coef.ptr, t.coef.data(), nnz * sizeof(double), cudaMemcpyHostToDevice,
+                                   c.stream));
+        FORGE_CUDA(cudaMemcpyAsync(x->v_code.ptr, t.code.data(), nnz * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    }
+    FORGE_CUDA(cudaMemcpyAsync(x->v_ph.ptr, ph.data(), ph.size() * sizeof(double2), cudaMemcpyHostToDevice, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    x->valley = true;
     return 0;
 }
 
@@ -1251,6 +1415,19 @@ int forge_gpu_get_fock(forge_ctx* x, double DegFactor, int64_t nOccStates, int64
         for (int t = 0; t < 4; ++t) st[q].wph[t] = cmul(bph[k * 4 + t], wgt);
     }
     if (nOccStates == 0) st.clear();
+    if (x->valley) {
+        // Main.f90:470-511: the averaged window plus zFockBulk, divided by Nk
+        const size_t NN = (size_t)c.N * c.N;
+        FORGE_TRY(x->Pn.ensure(4 * NN * sizeof(double2)));
+        FORGE_CUDA(cudaMemsetAsync(x->Pn.ptr, 0, 4 * NN * sizeof(double2), c.stream));
+        FORGE_TRY(valley_window(x, st));
+        FORGE_TRY(scf_combine(c, x->Pn.as<double2>(), c.bulk.as<double2>()));
+        x->have_pnew = true;
+        if (zFock)
+            FORGE_CUDA(cudaMemcpyAsync(zFock, x->Pn.ptr, 4 * NN * sizeof(double2), cudaMemcpyDeviceToHost, c.stream));
+        FORGE_CUDA(cudaStreamSynchronize(c.stream));
+        return 0;
+    }
     expand_c3_states(x, st);
     const int64_t nst = (int64_t)st.size();
     if (nst > 0) {
@@ -1439,7 +1616,7 @@ int forge_gpu_scf_iteration(forge_ctx* x, double* Energies, forge_iter_report* r
     int info = 0;
     FORGE_TRY(solve_device(x, &info, false));
     FORGE_TRY(sort_device(x, c.s.nfilling));
-    FORGE_TRY(project_fused(x));
+    FORGE_TRY(x->valley ? project_valley(x) : project_fused(x));
     FORGE_TRY(symmetrize_pnew(x));
     FORGE_TRY(scf_density(c, x->Pn.as<double2>(), x->dens_new.as<double>()));
     FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(),

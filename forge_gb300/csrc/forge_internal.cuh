@@ -168,6 +168,21 @@ int c3_build_tables(int64_t numk, int64_t N, int64_t nlayers, const int64_t* kco
 int launch_c3_rotate(cudaStream_t st, const double2* Xr, const double* wr, int64_t N, int64_t iu, int64_t nslots,
                      const int64_t* slot_tab, const int64_t* perm, const double2* phase, double2* X, double* w);
 
+// valley projection (valley.cu)
+struct ValleyTerms {
+    std::vector<int64_t> rowp, col;  // CSR rows of V(k) (N + 1) and column of each term
+    std::vector<double> coef;        // sign(cos 3 phi) / sqrt(27); the term is i coef phase
+    std::vector<int> code;           // phase: 0 home cell, c = 1..3 exp(-i k.R_c), 3 + c exp(+i k.R_c)
+};
+int valley_build_terms(const Context& c, const int64_t* RotateLayers, ValleyTerms& t);
+void valley_phases(const Context& c, std::vector<double2>& ph);
+int launch_valley_gram(cudaStream_t st, const double2* X, int64_t N, int64_t iu, int64_t c0, int64_t nb, int64_t Nk,
+                       const int64_t* rowp, const int64_t* col, const double* coef, const int* code,
+                       const double2* ph, double2* W, double2* G);
+int launch_valley_rotate(cudaStream_t st, const double2* X, int64_t N, int64_t iu, int64_t c0, int64_t nb, int64_t Nk,
+                         const double2* S, double2* Xv);
+int rr_small(int n, const double2* G, const double2* S, double* theta, double2* M);
+
 // symmetry switches of the SCF loop (symmetry.cu)
 int launch_symmetrize(cudaStream_t st, double2* P, double2* scratch, const int64_t* perm, int64_t N, bool T, bool C2,
                       bool C2T);

@@ -216,6 +216,14 @@ int forge_gpu_set_refinement(forge_ctx* ctx, int64_t width);
  * rotated copies.  Needs numk divisible by 3 and fphase = 0 (FORGE_ERR_ARG otherwise), and no k shard. */
 int forge_gpu_set_c3(forge_ctx* ctx, int64_t nenforceC3, const int64_t* nC3pairs, const int64_t* RotateLayers);
 
+/* nenforceValley (Setup.f90:31): 1 averages the window part of every new density matrix of the SCF
+ * loop (forge_gpu_scf_iteration, forge_gpu_get_fock; not the initial guess) with its valley
+ * transform, as Main.f90:470-500 does: GetFock over the window eigenvectors X and over X S(k),
+ * S(k) = sign(X^H V(k) X) with the valley operator V(k) of ValleyPhase (TightBinding.f90:60-157),
+ * each with weight 1/2.  RotateLayers (nlayers) gives each layer's rotation.  Not combined with the
+ * C3-reduced solve or a k shard (FORGE_ERR_ARG / FORGE_ERR_STATE). */
+int forge_gpu_set_valley(forge_ctx* ctx, int64_t nenforceValley, const int64_t* RotateLayers);
+
 /* nenforceT, nenforceC2, nenforceC2T (Setup.f90:28-30), each 0 (default) or 1: the symmetry
  * averages of Main.f90:513-534 on every new density matrix of forge_gpu_scf_iteration (not on the
  * initial guess), in the order T, C2, C2T.  nC2pairs (1-based, a permutation; C2_RelatedPoints,
