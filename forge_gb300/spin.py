@@ -1,6 +1,7 @@
 """Spin-polarised SCF (numS = 2) on two device contexts, one per spin.
 
-Main.f90:236-679 with numS = 2 and no symmetry enforcement.  Each spin has its own context.  That
+Main.f90:236-679 with numS = 2; the C3, valley and symmetry switches of the Setup act in each spin's
+context as in the numS = 1 path.  Each spin has its own context.  That
 context holds the spin's density matrix, solves H(k) with the spin's potential, and forms the
 spin's new density matrix.  These are the per-spin routines of the numS = 1 path, unchanged.  The
 host joins the spins:
@@ -146,6 +147,9 @@ class SpinPolarisedScf:
         deg = fl["DegFactor"]
         nocc, npart = fl["nOccStates"], fl["nPartOccStates"]
         Pn = [self.hf[sp].GetFock(deg, nocc[sp], npart[sp]) for sp in range(2)]
+        if self.setup.nenforceT or self.setup.nenforceC2 or self.setup.nenforceC2T:
+            # Main.f90:513-534 on each spin's new zFock
+            Pn = [self.hf[sp].Symmetrize() for sp in range(2)]
         dn_new = [density(p) for p in Pn]
         # OptimalStep (HartreeFock.f90:1148-1227) over the spin-summed energy
         c0 = self.total(self.E)

@@ -53,15 +53,21 @@ class OracleSpinEngine:
 
     def GetFock(self, DegFactor, nOccStates, nPartOccStates, copy_out=True):
         moms, sv = self.sorted
-        Pw = fo.get_fock(self.so, self.g, sv, moms, nOccStates, nPartOccStates, DegFactor)
-        return _to_F((Pw + self.sol["bulk"]) / complex(float(self.so.Nk), 0.0))
+        Pw = fo.window_fock(self.so, self.g, self.sol, sv, moms, nOccStates, nPartOccStates, DegFactor)
+        self.Pn = (Pw + self.sol["bulk"]) / complex(float(self.so.Nk), 0.0)
+        return _to_F(self.Pn)
+
+    def Symmetrize(self, copy_out=True):
+        self.Pn = fo.enforce_symmetries(self.so, self.g, self.Pn)
+        return _to_F(self.Pn)
 
 
-@pytest.mark.parametrize("split", [False, True])
-def test_spin_scf_host_logic_follows_the_oracle(lib, split):
+@pytest.mark.parametrize("split,flags", [(False, {}), (True, {}), (True, dict(nenforceT=1, nenforceC2=1)),
+                                         (True, dict(nenforceValley=1))])
+def test_spin_scf_host_logic_follows_the_oracle(lib, split, flags):
     import forge_gb300 as fg
     from forge_gb300.spin import SpinPolarisedScf
-    kw = dict(ntheta=1, numk=3, nfilling=2.0, degfactor_mode="corrected")
+    kw = dict(ntheta=1, numk=3, nfilling=2.0, degfactor_mode="corrected", **flags)
     so1 = fo.Setup(**kw)
     so2 = fo.Setup(numS=2, **kw)
     g = fo.build_geometry(so1)
