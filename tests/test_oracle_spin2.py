@@ -83,12 +83,15 @@ def _spin2(s1):
     return s2
 
 
-@pytest.mark.parametrize("nfilling,mode", [(0.0, "reference"), (2.0, "corrected"), (-1.0, "reference")])
-def test_spin_symmetric_state_reduces_to_numS1(nfilling, mode):
+@pytest.mark.parametrize("nfilling,mode,flags", [(0.0, "reference", {}), (2.0, "corrected", {}),
+                                                 (-1.0, "reference", {}), (2.0, "corrected", dict(nenforceC3=1)),
+                                                 (2.0, "corrected", dict(nenforceValley=1, nenforceC2T=1))])
+def test_spin_symmetric_state_reduces_to_numS1(nfilling, mode, flags):
     """With both spins equal, every numS = 2 quantity is the numS = 1 one: nFermiLevel doubles,
     the merged list pairs the spins, DegFactor, the energies (factor 3 - numS) and the potentials
-    (Main.f90:577-594) coincide, so the SCF trajectories agree exactly."""
-    s1 = fo.Setup(ntheta=1, numk=3, nfilling=nfilling, degfactor_mode=mode)
+    (Main.f90:577-594) coincide, so the SCF trajectories agree exactly; also with the C3, valley and
+    symmetry switches, which act on each spin alone."""
+    s1 = fo.Setup(ntheta=1, numk=3, nfilling=nfilling, degfactor_mode=mode, **flags)
     s2 = _spin2(s1)
     g = fo.build_geometry(s1)
     T = fo.pair_tables(s1, g)
