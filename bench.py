@@ -147,7 +147,8 @@ def run_ours(args, cfg, rank):
     fbuild.build()
     mixed = args.mode in ("fast", "mixed")
     S = fg.Setup(ntheta=cfg["ntheta"], numk=cfg["numk"], nfilling=cfg["nfilling"], epsilon=cfg["epsilon"],
-                 degfactor_mode=args.degfactor, precision="mixed" if mixed else "fp64")
+                 degfactor_mode=args.degfactor, precision="mixed" if mixed else "fp64",
+                 nenforceC3=1 if args.c3 else 0)
     t0 = time.time()
     hf = fg.HartreeFock(S)
     hf.set_mixing(args.mixer, args.mix_depth, args.mix_beta)
@@ -376,10 +377,16 @@ def main():
                          "taking the iteration counts from the recorded --converge run")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--c3", action="store_true",
+                    help="C3-reduced solve (nenforceC3 = 1; the workload's numk must be a multiple of 3)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    cfg = CONFIGS[args.config]
+    cfg = dict(CONFIGS[args.config])
+    if args.c3:
+        if cfg["numk"] % 3:
+            ap.error("--c3 needs a k grid with numk divisible by 3")
+        cfg["name"] += "_c3"
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     pg = None
