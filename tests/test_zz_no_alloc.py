@@ -4,7 +4,8 @@ It exists for callers that cannot allocate device memory when they call the solv
 or arena owning the GPU, latency-critical loops, hosts that manage all device buffers); its
 workspace is a static device array.  Two calls in a row through the C-ABI must agree with the
 existing entry point forge_gpu_zheevr_batch within the FP64 tolerances the other tests use
-(eigenvalues 1e-12 relative, eigenvector projectors 1e-10).  This file is collected last.
+(eigenvalues 1e-12 relative, eigenvector projectors 1e-10).  This file is collected after the
+per-routine parity files.
 """
 import ctypes as C
 
