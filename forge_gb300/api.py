@@ -430,6 +430,12 @@ class HartreeFock:
                       allow_info=True)
         return B, E, FB, info
 
+    def GetBands(self) -> np.ndarray:
+        """Bands (numb, Nk) of the last solve (the window eigenvalues nLower..nUpper per k)."""
+        B = np.zeros((self.numb, self.Nk), order="F")
+        _check(self.lib.forge_gpu_get_bands(self.ctx, _ptr(B)))
+        return B
+
     def SortEnergies_1Spin(self):
         """HartreeFock.f90:885-925: (SortedEnergies, nSortedMomenta, sorted flat icount)."""
         n = self.numb * self.Nk

@@ -23,7 +23,9 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-from .api import Geometry, HartreeFock, Setup, build_geometry, fermi_2spins
+import os
+
+from .api import Geometry, HartreeFock, Setup, build_geometry, fermi_2spins, parameters_string, plot_bands, write_fock
 
 
 @dataclasses.dataclass
@@ -39,6 +41,10 @@ class SpinIteration:
     nOccStates: tuple
     nPartOccStates: tuple
     DegFactor: float
+    KineticEnergyIn: float = 0.0     # summed over the spins
+    FockEnergyIn: float = 0.0        # summed over the spins
+    HartreeEnergyIn: float = 0.0
+    HubbardEnergyIn: float = 0.0
 
 
 def hartree_hubbard(LR: np.ndarray, dens: Sequence[np.ndarray]) -> tuple:
@@ -73,9 +79,11 @@ class SpinPolarisedScf:
         self.setup = setup
         self.s = setup.to_struct()
         one = dataclasses.replace(setup, numS=1)
+        self.geometry = geometry
         if engines is None:
-            g = geometry if geometry is not None else build_geometry(one)
-            engines = [HartreeFock(one, g), HartreeFock(one, g)]
+            if self.geometry is None:
+                self.geometry = build_geometry(one)
+            engines = [HartreeFock(one, self.geometry), HartreeFock(one, self.geometry)]
             self._own = True
         else:
             self._own = False
@@ -174,19 +182,52 @@ class SpinPolarisedScf:
             self.hf[sp].SetState(P[sp])
         self.V = potentials(self.LR, dens, s.alphaH, s.U)
         return SpinIteration(it, dn, step, self.total(Ein), self.total(E), fl["FermiEnergy"], tuple(nocc),
-                             tuple(npart), deg)
+                             tuple(npart), deg, *Ein)
 
-    def run(self, itmax: int, density_tol: float = 0.0, P_init: Optional[Sequence[np.ndarray]] = None) -> list:
+    def run(self, itmax: int, density_tol: float = 0.0, P_init: Optional[Sequence[np.ndarray]] = None,
+            output_dir: Optional[str] = None, fock_dir: Optional[str] = None, statename: str = "SSS") -> list:
         """The SCF loop: itmax iterations (the reference's stop), or fewer once DensityConvergence
-        drops below ``density_tol`` (> 0)."""
+        drops below ``density_tol`` (> 0).
+
+        With ``output_dir`` every iteration appends to Energy<parameters> and Convergence<parameters>
+        and rewrites Bands-nspin1/2<parameters> (Main.f90:596-639, numS = 2 columns: the energies
+        summed over the spins); with ``fock_dir`` it rewrites Fock-nspin1/2<parameters> in the
+        reference's record order (Main.f90:645-672)."""
         if P_init is not None:
             self.set_state(P_init)
         elif self.P is None:
             self.plain_guess()
+        params = parameters_string(self.setup, statename) if (output_dir or fock_dir) else ""
+        fe = fc = None
+        if output_dir:
+            fe = open(os.path.join(output_dir, "Energy" + params), "w")
+            fc = open(os.path.join(output_dir, "Convergence" + params), "w")
         reports = []
-        for it in range(1, itmax + 1):
-            r = self.iterate(it)
-            reports.append(r)
-            if density_tol > 0 and r.DensityConvergence < density_tol:
-                break
+        try:
+            for it in range(1, itmax + 1):
+                r = self.iterate(it)
+                reports.append(r)
+                if output_dir:
+                    self._write_outputs(r, output_dir, params, fe, fc)
+                if fock_dir:
+                    for sp in range(2):
+                        write_fock(self.setup, self.P[sp], os.path.join(fock_dir, f"Fock-nspin{sp + 1}" + params))
+                if density_tol > 0 and r.DensityConvergence < density_tol:
+                    break
+        finally:
+            for f in (fe, fc):
+                if f is not None:
+                    f.close()
         return reports
+
+    def _write_outputs(self, r: SpinIteration, output_dir: str, params: str, fe, fc):
+        g = self.geometry if self.geometry is not None else build_geometry(dataclasses.replace(self.setup, numS=1))
+        for sp in range(2):
+            plot_bands(self.setup, g, self.hf[sp].GetBands(), r.FermiEnergy,
+                       os.path.join(output_dir, f"Bands-nspin{sp + 1}" + params))
+        fc.write(f"{float(r.it):5.1f}   {r.DensityConvergence:9.6f}   {r.Step:5.3f}   "
+                 f"{r.TotalEnergyIn - r.TotalEnergy:24.9f}   \n")
+        fe.write(f"{float(r.it):5.1f}   {r.TotalEnergyIn:24.9f}   {r.KineticEnergyIn:24.9f}   "
+                 f"{r.FockEnergyIn:24.9f}   {r.HartreeEnergyIn:24.9f}   {r.HubbardEnergyIn:24.9f}   \n")
+        fe.flush()
+        fc.flush()

@@ -46,6 +46,9 @@ class OracleSpinEngine:
         self.sol = fo.solve(self.so, self.g, self.T, np.asarray(Potential), self.P)
         return None, None, None, 0
 
+    def GetBands(self):
+        return np.asfortranarray(self.sol["bands"])
+
     def SortEnergies_1Spin(self):
         se, idx, moms, sv, _, _ = fo.sort_energies_1spin(self.so, self.g, self.sol["bands"], self.sol["evecs"])
         self.sorted = (moms, sv)
@@ -99,3 +102,41 @@ def test_spin_scf_rejects_numS1(lib):
     from forge_gb300.spin import SpinPolarisedScf
     with pytest.raises(ValueError):
         SpinPolarisedScf(fg.Setup(ntheta=1, numk=3), engines=[None, None])
+
+
+def test_spin_scf_output_files(lib, tmp_path):
+    """Energy / Convergence / Bands-nspin1,2 / Fock-nspin1,2 files of a numS = 2 run (Main.f90:596-672):
+    the numS = 2 columns, one line per iteration, and Fock files that read back to the state."""
+    import forge_gb300 as fg
+    from forge_gb300.spin import SpinPolarisedScf
+    kw = dict(ntheta=1, numk=3, nfilling=2.0, degfactor_mode="corrected")
+    so1 = fo.Setup(**kw)
+    g = fo.build_geometry(so1)
+    T = fo.pair_tables(so1, g)
+    LR = fo.long_range_interaction(so1, g)
+    S2 = fg.Setup(numS=2, **kw)
+    scf = SpinPolarisedScf(S2, geometry=fg.build_geometry(fg.Setup(**kw)),
+                           engines=[OracleSpinEngine(so1, g, T, LR) for _ in range(2)])
+    out, fock = tmp_path / "output", tmp_path / "dataFock"
+    out.mkdir()
+    fock.mkdir()
+    reps = scf.run(2, output_dir=str(out), fock_dir=str(fock))
+    params = fg.parameters_string(S2)
+    assert "-numS2-" in params
+    energy = (out / ("Energy" + params)).read_text().splitlines()
+    conv = (out / ("Convergence" + params)).read_text().splitlines()
+    assert len(energy) == len(conv) == 2
+    for line_e, line_c, r in zip(energy, conv, reps):
+        e = [float(x) for x in line_e.split()]
+        c = [float(x) for x in line_c.split()]
+        assert e[0] == r.it and c[0] == r.it
+        assert e[1:] == pytest.approx([r.TotalEnergyIn, r.KineticEnergyIn, r.FockEnergyIn, r.HartreeEnergyIn,
+                                       r.HubbardEnergyIn], abs=1e-9)
+        assert c[1:] == pytest.approx([r.DensityConvergence, r.Step, r.TotalEnergyIn - r.TotalEnergy], abs=1e-6)
+    for sp in (1, 2):
+        assert (out / (f"Bands-nspin{sp}" + params)).stat().st_size > 0
+        back = fg.read_fock(S2, str(fock / (f"Fock-nspin{sp}" + params)))
+        Pf = scf.P[sp - 1]
+        low = np.tril(np.ones((S2.to_struct().ndim,) * 2, bool))
+        assert np.array_equal(back[:, :, 0][low], Pf[:, :, 0][low])
+        assert np.array_equal(back[:, :, 1:], Pf[:, :, 1:])
