@@ -25,7 +25,8 @@ import numpy as np
 
 import os
 
-from .api import Geometry, HartreeFock, Setup, build_geometry, fermi_2spins, parameters_string, plot_bands, write_fock
+from .api import (Geometry, HartreeFock, Setup, build_geometry, fermi_2spins, parameters_string, plot_bands, read_fock,
+                  write_fock)
 
 
 @dataclasses.dataclass
@@ -138,6 +139,17 @@ class SpinPolarisedScf:
         self.dens = [density(p) for p in self.P]
         self.E = self.energies(self.P, self.dens)
         self.V = potentials(self.LR, self.dens, self.s.alphaH, self.s.U)
+
+    def read_state(self, fock_dir: str, setup_in: Optional[Setup] = None, statename_in: str = "SSS",
+                   record_bytes: int = 16):
+        """Checkpoint resume (nRead = 1, Main.f90:186-234): both spins' zFock from the Fock-nspin files
+        of the run described by ``setup_in`` (default: this run's setup); a numS = 1 checkpoint
+        (Fock-nspin1) starts both spins."""
+        sin = self.setup if setup_in is None else setup_in
+        params = parameters_string(sin, statename_in)
+        P = [read_fock(self.setup, os.path.join(fock_dir, f"Fock-nspin{1 if sin.numS == 1 else sp + 1}" + params),
+                       record_bytes) for sp in range(2)]
+        self.set_state(P)
 
     # -- one SCF iteration (Main.f90:365-595)
     def iterate(self, it: int = 0) -> SpinIteration:

@@ -140,3 +140,36 @@ def test_spin_scf_output_files(lib, tmp_path):
         low = np.tril(np.ones((S2.to_struct().ndim,) * 2, bool))
         assert np.array_equal(back[:, :, 0][low], Pf[:, :, 0][low])
         assert np.array_equal(back[:, :, 1:], Pf[:, :, 1:])
+
+
+def test_spin_scf_resumes_from_fock_files(lib, tmp_path):
+    """nRead = 1 (Main.f90:186-234): a numS = 2 checkpoint gives each spin its own file; a numS = 1
+    checkpoint starts both spins from Fock-nspin1."""
+    import forge_gb300 as fg
+    from forge_gb300.spin import SpinPolarisedScf
+    kw = dict(ntheta=1, numk=3, nfilling=2.0, degfactor_mode="corrected")
+    so1 = fo.Setup(**kw)
+    g = fo.build_geometry(so1)
+    T = fo.pair_tables(so1, g)
+    LR = fo.long_range_interaction(so1, g)
+    S1, S2 = fg.Setup(**kw), fg.Setup(numS=2, **kw)
+
+    def make():
+        return SpinPolarisedScf(S2, engines=[OracleSpinEngine(so1, g, T, LR) for _ in range(2)])
+
+    a = make()
+    P0 = np.stack([fo.plain_guess(fo.Setup(**{**kw, "nfilling": kw["nfilling"] + d}), g, T)[0] for d in (1.0, -1.0)])
+    a.run(1, P_init=[_to_F(p) for p in P0], fock_dir=str(tmp_path))
+    b = make()
+    b.read_state(str(tmp_path))
+    low = np.tril(np.ones(a.P[0].shape[:2], bool))
+    for sp in range(2):
+        # the file holds the lower triangle of R = 0 (the upper is its conjugate) and the other cells in full
+        assert np.array_equal(b.P[sp][:, :, 0][low], a.P[sp][:, :, 0][low])
+        assert np.array_equal(b.P[sp][:, :, 1:], a.P[sp][:, :, 1:])
+    assert not np.array_equal(b.P[0], b.P[1])
+    # a numS = 1 checkpoint starts both spins alike
+    fg.write_fock(S1, _to_F(P0[0]), str(tmp_path / ("Fock-nspin1" + fg.parameters_string(S1))))
+    c = make()
+    c.read_state(str(tmp_path), setup_in=S1)
+    assert np.array_equal(c.P[0], c.P[1])
