@@ -2,23 +2,30 @@
 
 One step = one SCF iteration of the hot path (H(k) assembly for all k, batched eigen-solve of
 eigenpairs 1..N/2+10, density-matrix projectors, sort / Fermi level, energies, mixing and Hartree
-potential) with every array resident in HBM, timed with CUDA events on the library's stream.
+potential) with every array resident in HBM.
 
-value = time-to-SCF: the starting guess, then the SCF iterations until the mean-field residual is
-below --tol (1e-6 eV).  W warm-up iterations are charged at the timed mean of their precision; the K
-timed iterations and every later one at their own event time.  With --converge the run continues
-to the tolerance; otherwise the iteration counts (and, if this run did none, the FP64 iteration
-time) come from the recorded --converge run of the same workload, mode, DegFactor rule and mixer in
-profiles/scf_records.json, and config.iterations_source says so.
+Timed region (CUDA events on the library's stream, cumulative from one start event): the starting
+guess, then exactly K SCF iterations.  value = time-to-SCF = the event time from the start of the
+guess to the end of the first iteration whose mean-field residual is below --tol (1e-6 eV).  If
+the K steps end before that, the same SCF continues (every iteration still event-timed) until it
+converges, reaches --itmax or the --budget-s wall-clock budget; config.converged says which.
+Before the timed region, W warm-up steps run the same guess and W iterations; the timed SCF then
+starts again from its guess, so the warm-up does not shorten it.
 
-Modes: fast = learned warm start + mixed-precision iterations + FP64 finish; mixed = plain guess +
-mixed + FP64 finish; plain = plain guess + FP64.  Mixers: Anderson/Pulay (depth 6, default) or the
-reference's OptimalStep.
+e2e: the same SCF again, end to end through the reference-facing C-ABI calls with pinned host
+buffers, the way a Fortran host would drive it (forge_gpu_solve with host Potential / zFock in and
+Bands, zEigenvectors, zFockBulk out; sort; Fermi level; forge_gpu_get_fock with P_new out;
+forge_gpu_optimal_step; forge_gpu_mix_potential; forge_gpu_get_state with zFock, Density and
+Potential out), wall-clock timed from the guess to the converging iteration.
+
+Modes: fast = learned warm start + mixed-precision eigen-solve with the FP64-accurate eigenpair
+refinement; mixed = plain guess + the same mixed path; plain = plain guess + FP64.  The mixer is
+Anderson/Pulay (depth 6) unless --mixer oda (the reference's OptimalStep).
 
 Workloads: 4 = 1.05 deg twisted bilayer, m=31, N=11908, 4x4 k, nu=+2, eps=10 (headline, default);
 1 = m=10, N=1324, 12x12 k, nu=+2; 2 = m=20, N=5044, 8x8 k, nu=-2, eps=8; 0 = m=5, N=364, 6x6 k,
 nu=0.  Inputs are synthetic by construction (the geometry and the model are generated from the
-parameters); nothing is read from disk.
+parameters); nothing is read from disk except the warm-start network weights.
 """
 from __future__ import annotations
 
@@ -44,6 +51,24 @@ CONFIGS = {
 }
 METRIC = "time-to-SCF (s) and SCF iters, 1.05deg TBG: net+mixed vs plain FP64, same accuracy"
 
+# Plain FP64 GPU SCF runs measured to convergence with `--mode plain --converge` (Pulay depth 6,
+# beta 0.7, corrected DegFactor).  They are reported in the labelled field plain_fp64_recorded and
+# give the reference arm its iteration count; they never enter `value`.
+PLAIN_FP64_RECORDED = {
+    "tbg_m10_N1324_12x12_nu+2_eps10": {
+        "iterations": 6, "time_to_scf_s": 36.1, "ms_per_iter": 5160.0, "converged": True,
+        "final_residual": 1.0e-07, "date": "2026-12-03",
+        "command": "python bench.py --config 1 --mode plain --converge"},
+}
+
+# DRAM traffic of the dominant kernels per algorithmic byte, from ncu captures small enough for the
+# profiler (dram__bytes_read.sum + dram__bytes_write.sum over the work model's bytes).
+NCU_TRAFFIC_RATIO = {
+    "hemv": (1.044, "ncu --set full of k_trd_hemv<float> at N=5044, column 1501 (n'=3543): 52.25 MB read + "
+                    "0.19 MB written against 50.23 MB algorithmic (trailing lower triangle, complex64); "
+                    "python -m forge_gb300.eigbench --m 20 --precision mixed"),
+}
+
 
 def _peaks():
     try:
@@ -55,7 +80,7 @@ def _peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling during the timed region (reads only)."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -108,216 +133,189 @@ def _pinned(shape, dtype):
     n = int(np.prod(shape)) * np.dtype(dtype).itemsize
     p = C.c_void_p()
     if rt.cudaHostAlloc(C.byref(p), C.c_size_t(n), 0) != 0:
-        return np.zeros(shape, dtype=dtype, order="F")
+        raise RuntimeError(f"cudaHostAlloc of {n} bytes failed")
     buf = (C.c_byte * n).from_address(p.value)
     return np.ndarray(shape, dtype=dtype, buffer=buf, order="F")
 
 
-def _traffic(stage: str, alg_bytes_per_launch: float):
-    """DRAM bytes per launch of `stage`: the ncu-measured ratio of DRAM traffic to algorithmic bytes
-    (profiles/traffic.json, from a capture small enough for ncu) times this run's algorithmic bytes."""
-    try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            t = json.load(f)[stage]
-        return {"bytes_per_launch": float(t["ratio"]) * alg_bytes_per_launch, "ratio_to_algorithmic": t["ratio"],
-                "source": t["source"]}
-    except Exception:
-        return None
+def _log(obj):
+    print(json.dumps(obj), file=sys.stderr, flush=True)
 
 
-def _scf_record(workload: str, mode: str, degfactor: str, mixer: str):
-    """Iteration counts of a recorded --converge run (profiles/scf_records.json)."""
-    try:
-        with open(os.path.join(ROOT, "profiles", "scf_records.json")) as f:
-            return json.load(f)[workload][f"{mode}/{degfactor}/{mixer}"]
-    except Exception:
-        return None
-
-
-def run_ours(args, cfg, rank):
-    """Runs the SCF of the workload from its starting guess to the residual tolerance.
-
-    Every iteration is timed with CUDA events on the library stream.  The first W iterations
-    are the untimed warm-up, the next K the timed steps; the remaining iterations continue
-    the same SCF until the mean-field residual is below the tolerance (or itmax).  The
-    time-to-SCF charges the guess, the warm-up iterations at the timed mean of their
-    precision, and every later iteration at its own event-timed duration."""
+def _make(args, cfg):
     import forge_gb300 as fg
-    from forge_gb300 import build as fbuild
-    fbuild.build()
     mixed = args.mode in ("fast", "mixed")
     S = fg.Setup(ntheta=cfg["ntheta"], numk=cfg["numk"], nfilling=cfg["nfilling"], epsilon=cfg["epsilon"],
                  degfactor_mode=args.degfactor, precision="mixed" if mixed else "fp64",
                  nenforceC3=1 if args.c3 else 0)
-    t0 = time.time()
     hf = fg.HartreeFock(S)
     hf.set_mixing(args.mixer, args.mix_depth, args.mix_beta)
+    if mixed:
+        hf.set_refinement(args.rr_width)
     hf.LongRangeInteraction(copy_out=False)
     hf.synchronize()
-    t_setup = time.time() - t0
-    hf.mark(0)
-    if args.mode == "fast":
+    return S, hf
+
+
+def _guess(hf, S, mode):
+    """Starting guess: the learned warm start (fast) or the reference's plain guess."""
+    if mode == "fast":
         from forge_gb300 import warmstart
         E0 = warmstart.apply(hf, S)
-    else:
-        E0, _ = hf.PlainGuess()
+        return list(E0), {"warm_start_used": bool(hf.warm_start_used),
+                          "warm_start_residuals": list(hf.warm_start_residuals)}
+    E0, _ = hf.PlainGuess()
+    return list(E0), {}
+
+
+def scf_device(hf, S, args, n_steps, budget_s, t_start_wall, profile=False):
+    """The device-resident SCF from its guess: n_steps iterations, then (if it has not converged)
+    more until it converges, itmax or the wall-clock budget.  Returns the per-iteration records with
+    cumulative CUDA-event times from the start of the guess."""
+    hf.mark(0)
+    E, ginfo = _guess(hf, S, args.mode)
     hf.mark(1)
-    hf.synchronize()
     t_guess = hf.elapsed_ms(0, 1) / 1e3
-    E = list(E0)
-    hist = []       # per-iteration report + precision + event-timed ms
-    prec = "mixed" if mixed else "fp64"
-    hf.set_precision(prec)
-
-    best = [1e300, 0]   # best mixed residual, iterations since it improved by a factor 0.8
-
-    def iterate():
-        nonlocal E, prec
-        used = prec
-        hf.mark(0)
+    if profile:
+        hf.profile(True)
+    hist = []
+    t_conv = None
+    launches0 = hf.lib.forge_gpu_launch_count()
+    timed_info = {}
+    while True:
+        i = len(hist)
+        if i == n_steps:
+            timed_info = {"launches": hf.lib.forge_gpu_launch_count() - launches0}
+            if profile:
+                timed_info["prof"] = hf.profile_read()
+                hf.profile(False)
+        if i >= n_steps and (t_conv is not None or i >= args.itmax or time.time() - t_start_wall > budget_s):
+            break
+        slot = 2 + (i % 60)
         rep, E, info = hf.ScfIteration(E)
-        hf.mark(1)
-        rep = dict(rep, precision=used, ms=hf.elapsed_ms(0, 1))
-        hist.append(rep)
-        # progress on stderr: a long --converge run that is cut off still leaves its trajectory
-        print(json.dumps({"iter": len(hist), "precision": used, "ms": round(rep["ms"], 1),
-                          "residual": rep["residual"], "TotalEnergy": rep["TotalEnergy"],
-                          "nPartOccStates": rep["nPartOccStates"]}), file=sys.stderr, flush=True)
-        if rep["residual"] < 0.8 * best[0]:
-            best[0], best[1] = rep["residual"], 0
-        else:
-            best[1] += 1
-        # mixed until the switch tolerance, or until the residual stalls near the FP32 noise floor
-        # (within 100x the switch tolerance; a slow SCF far from it is not a stall)
-        if used == "mixed" and (rep["residual"] < args.switch_tol or
-                                (best[1] >= 3 and rep["residual"] < 100 * args.switch_tol)):
-            prec = "fp64"
-            hf.set_precision(prec)
-        return rep
+        hf.mark(slot)
+        t_cum = hf.elapsed_ms(0, slot) / 1e3
+        prev = hist[-1]["t_cum"] if hist else t_guess
+        rec = {"iter": i + 1, "ms": (t_cum - prev) * 1e3, "t_cum": t_cum, "residual": rep["residual"],
+               "TotalEnergy": rep["TotalEnergy"], "nPartOccStates": rep["nPartOccStates"], "info": info}
+        hist.append(rec)
+        _log({k: (round(v, 1) if k == "ms" else v) for k, v in rec.items() if k != "t_cum"})
+        if t_conv is None and rep["residual"] < args.tol:
+            t_conv = t_cum
+    return dict(t_guess=t_guess, hist=hist, t_conv=t_conv, guess_info=ginfo, E=E, **timed_info)
 
-    for _ in range(args.warmup):
-        iterate()
-    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
-    clocks.start()
-    hf.profile(True)
-    n_launch0 = hf.lib.forge_gpu_launch_count()
-    for _ in range(args.steps):
-        iterate()
-    hf.synchronize()
-    n_launch = hf.lib.forge_gpu_launch_count() - n_launch0
-    prof = hf.profile_read()
-    hf.profile(False)
-    clk = clocks.stop()
-    timed = hist[args.warmup:args.warmup + args.steps]
-    step_ms = [h["ms"] for h in timed]
-    # --converge: continue the same SCF to the residual tolerance (every iteration measured);
-    # otherwise the iteration counts (and the FP64 iteration time, when this run did none) come
-    # from the recorded --converge run of the same workload and mode
-    if args.converge:
-        while hist[-1]["residual"] >= args.tol and len(hist) < args.itmax:
-            iterate()
-    mean_by_prec = {}
-    for pr in ("mixed", "fp64"):
-        xs = [h["ms"] for h in hist[args.warmup:] if h["precision"] == pr]
-        if xs:
-            mean_by_prec[pr] = float(np.mean(xs))
-    record = None
-    if args.converge:
-        converged = hist[-1]["residual"] < args.tol
-        t_scf = t_guess
-        for i, h in enumerate(hist):
-            if i < args.warmup:
-                t_scf += mean_by_prec.get(h["precision"], h["ms"]) / 1e3
-            else:
-                t_scf += h["ms"] / 1e3
-        n_mixed = sum(1 for h in hist if h["precision"] == "mixed")
-        n_fp64 = sum(1 for h in hist if h["precision"] == "fp64")
-        source = "measured: this run continued the SCF to the tolerance"
-    else:
-        record = _scf_record(cfg["name"], args.mode, args.degfactor, args.mixer)
-        if record is None:
-            raise SystemExit(f"no recorded --converge run for {cfg['name']} / {args.mode}: run with --converge")
-        n_mixed, n_fp64 = int(record["n_mixed"]), int(record["n_fp64"])
-        ms_fp64 = mean_by_prec.get("fp64", float(record.get("ms_fp64", 0.0)))
-        ms_mixed = mean_by_prec.get("mixed", float(record.get("ms_mixed", 0.0)))
-        t_scf = t_guess + (n_mixed * ms_mixed + n_fp64 * ms_fp64) / 1e3
-        converged = bool(record.get("converged", False))
-        source = ("iteration counts" + ("" if "fp64" in mean_by_prec or n_fp64 == 0 else " and FP64 iteration time")
-                  + " from the recorded --converge run (profiles/scf_records.json); per-iteration times of this run")
-        if not converged:
-            source += ("; the recorded run did NOT reach the tolerance, so value is a lower bound of the "
-                       "time-to-SCF: " + str(record.get("note", "")))
-    # e2e: the reference-facing per-iteration calls with host buffers (pinned), copies included
-    e2e_ms = []
+
+def scf_e2e(hf, S, args, budget_s):
+    """The SCF through the reference-facing C-ABI calls with pinned host buffers (wall clock)."""
+    lib, ctx = hf.lib, hf.ctx
     N, Nk, numb = hf.N, hf.Nk, hf.numb
     Ph = _pinned((N, N, 4), np.complex128)
+    Pn = _pinned((N, N, 4), np.complex128)
+    FBh = _pinned((N, N, 4), np.complex128)
     Vh = _pinned((N,), np.float64)
     Dh = _pinned((N,), np.float64)
     Bh = _pinned((numb, Nk), np.float64)
     Zh = _pinned((N, numb, Nk), np.complex128)
-    FBh = _pinned((N, N, 4), np.complex128)
-    Pn = _pinned((N, N, 4), np.complex128)
-    lib = hf.lib
     ptr = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
-    lib.forge_gpu_get_state(hf.ctx, ptr(Ph), ptr(Dh), ptr(Vh))
     h2d = Ph.nbytes + Vh.nbytes
     d2h = Bh.nbytes + Zh.nbytes + FBh.nbytes + Pn.nbytes + Ph.nbytes + Dh.nbytes + Vh.nbytes
-    if mixed:
-        hf.set_precision("mixed")   # the copies' overhead does not depend on the precision
-    e2e_prec = "mixed" if mixed else "fp64"
-    for k in range(max(1, min(args.steps, args.e2e_steps))):
-        hf.synchronize()
-        t0 = time.perf_counter()
-        lib.forge_gpu_solve(hf.ctx, ptr(Vh), ptr(Ph), ptr(Bh), ptr(Zh), ptr(FBh))
-        lib.forge_gpu_sort_energies(hf.ctx, None, None, None)
+    import forge_gb300.api as api
+    hf.synchronize()
+    t0 = time.perf_counter()
+    E, _ = _guess(hf, S, args.mode)
+    api._check(lib.forge_gpu_get_state(ctx, ptr(Ph), ptr(Dh), ptr(Vh)))
+    hist = []
+    t_conv = None
+    t_start = time.time()
+    while len(hist) < args.itmax and time.time() - t_start < budget_s:
+        api._check(lib.forge_gpu_solve(ctx, ptr(Vh), ptr(Ph), ptr(Bh), ptr(Zh), ptr(FBh)), allow_info=True)
+        api._check(lib.forge_gpu_sort_energies(ctx, None, None, None))
         nf, ef, no, npart, deg = hf.FermiLevel()
-        lib.forge_gpu_get_fock(hf.ctx, C.c_double(deg), no, npart, ptr(Pn))
+        api._check(lib.forge_gpu_get_fock(ctx, C.c_double(deg), no, npart, ptr(Pn)))
         step, E = hf.OptimalStep(E)
-        hf.MixPotential(step)
-        lib.forge_gpu_get_state(hf.ctx, ptr(Ph), ptr(Dh), ptr(Vh))
-        hf.synchronize()
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        dn, res = hf.MixPotential(step)
+        api._check(lib.forge_gpu_get_state(ctx, ptr(Ph), ptr(Dh), ptr(Vh)))
+        t = time.perf_counter() - t0
+        hist.append({"iter": len(hist) + 1, "t_cum": t, "residual": res})
+        _log({"e2e_iter": len(hist), "t_cum_s": round(t, 2), "residual": res})
+        if res < args.tol:
+            t_conv = t
+            break
+    return dict(hist=hist, t_conv=t_conv, h2d=h2d, d2h=d2h,
+                per_iter_s=(hist[-1]["t_cum"] / len(hist)) if hist else None)
+
+
+def run_ours(args, cfg):
+    import forge_gb300 as fg
+    from forge_gb300 import build as fbuild
+    fbuild.build()
+    t_wall0 = time.time()
+    S, hf = _make(args, cfg)
+    t_setup = time.time() - t_wall0
+    # warm-up: the guess and W iterations, untimed
+    E, _ = _guess(hf, S, args.mode)
+    for _ in range(args.warmup):
+        rep, E, _ = hf.ScfIteration(E)
+        _log({"warmup_iter": _ + 1, "residual": rep["residual"]})
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    run = scf_device(hf, S, args, args.steps, args.budget_s, t_wall0, profile=True)
+    clk = clocks.stop()
+    hf.profile(False)
+    state = None
+    if args.save_state:
+        state = _state_summary(hf, S)
+    e2e = None
+    if not args.no_e2e:
+        e2e = scf_e2e(hf, S, args, max(60.0, args.budget_s - (time.time() - t_wall0)))
+    N, Nk = hf.N, hf.Nk
     hf.close()
-    t_iter = float(np.mean(step_ms)) / 1e3
-    # e2e time-to-SCF: every iteration pays the measured host-copy overhead of the e2e calls
-    overhead_ms = max(0.0, float(np.mean(e2e_ms)) - mean_by_prec.get(e2e_prec, float(np.mean(e2e_ms))))
-    t_scf_e2e = t_scf + len(hist) * overhead_ms / 1e3
-    return dict(t_iter=t_iter, step_ms=step_ms, iters=n_mixed + n_fp64, converged=converged,
-                residual=hist[-1]["residual"], source=source, record=record,
-                prof=prof, clocks=clk, launches=n_launch, e2e_iter=float(np.mean(e2e_ms)) / 1e3,
-                e2e_overhead_ms=overhead_ms, t_scf_e2e=t_scf_e2e,
-                e2e_precision=e2e_prec, h2d=h2d, d2h=d2h, t_setup=t_setup, t_guess=t_guess, t_scf=t_scf,
-                mean_by_prec=mean_by_prec, N=N, Nk=Nk, hist=hist, n_mixed=n_mixed, n_fp64=n_fp64)
+    return dict(run=run, clocks=clk, e2e=e2e, t_setup=t_setup, N=N, Nk=Nk, state=state,
+                wall_s=time.time() - t_wall0)
+
+
+def _state_summary(hf, S):
+    """Converged-state summary (energies, bands, site densities, potential, order parameters and
+    P(R) on the short bonds) for comparing SCF runs that cannot share a 9 GB density matrix."""
+    from forge_gb300 import warmstart
+    P, dens, V = hf.GetState()
+    bands = hf.GetBands()
+    g = hf.geometry
+    op = hf.OrderParameters()
+    bonds = warmstart.bond_list(S, g)
+    pb = P[bonds[:, 0], bonds[:, 1], bonds[:, 2]]
+    return dict(dens=dens, V=V, bands=bands, order=np.array([op[k] for k in sorted(op)]),
+                order_names=np.array(sorted(op)), bonds=bonds, P_bonds=pb)
 
 
 def cpu_sample(cfg, n_max=2000):
-    """Oracle (port) timing of one SCF iteration on the host cores, from a bounded sample.
-
-    The sample is one k point: assembly of H(k) with ft / fv evaluated per pair as the reference
-    does, zheevr (range I), the ZHERK bulk projector, and one energy evaluation of the ODA pass
-    (counted 3 times per iteration).  Above n_max orbitals it runs on the principal n_max x n_max
-    block (the first n_max sites), and each part is scaled by its exact order in N: N^2 for the
-    pair loops, N^3 for zheevr with iu = N/2 + 10 and for the rank-(N/2) projector.  The k point is
-    then scaled by Nk."""
+    """Bounded CPU sample (the cpu_baseline leg): one SCF iteration of the oracle port estimated from
+    one k point on the principal n_max x n_max block of the sites (H(k) with ft / fv per pair as the
+    reference evaluates them, zheevr il=1..n/2+10, ZHERK bulk projector, one energy pass), each part
+    scaled to N by its exact order (N^2 for the pair loops, N^3 for zheevr and the projector), times
+    Nk (+ 3 energy passes)."""
     from oracle import forge_oracle as fo
-    import scipy.linalg.blas as blas
     import forge_gb300 as fg
-    so = fo.Setup(ntheta=cfg["ntheta"], numk=cfg["numk"], nfilling=cfg["nfilling"], epsilon=cfg["epsilon"])
-    # the sites come from the host geometry code (bit-identical to the oracle's, and seconds instead
-    # of a minute at N = 11908); geometry is set-up work outside the timed iteration
     g = fg.build_geometry(fg.Setup(ntheta=cfg["ntheta"], numk=cfg["numk"], nfilling=cfg["nfilling"],
                                    epsilon=cfg["epsilon"]))
+    so = fo.Setup(ntheta=cfg["ntheta"], numk=cfg["numk"], nfilling=cfg["nfilling"], epsilon=cfg["epsilon"])
+    return _cpu_k_point(fo, so, np.asarray(g.Coords), g.nUnitCell_1, g.nUnitCell_2, g.tn[:, 0], g.tn[:, 1],
+                        g.MomentaValues[0, min(1, cfg["numk"] - 1)], n_max)
+
+
+def _cpu_k_point(fo, so, coords, u1, u2, t1, t2, vk, n_max):
+    import scipy.linalg.blas as blas
     lib = fo._clib()
     if lib is None:
         return None
     N = so.ndim
     Ns = min(N, n_max)
-    X = np.ascontiguousarray(np.asarray(g.Coords)[:Ns])
+    X = np.ascontiguousarray(coords[:Ns])
     mdl = fo._model_struct(so)
-    u1 = np.ascontiguousarray(g.nUnitCell_1, dtype=np.int64)
-    u2 = np.ascontiguousarray(g.nUnitCell_2, dtype=np.int64)
-    t1, t2 = np.array(g.tn[:, 0]), np.array(g.tn[:, 1])
-    vk = np.ascontiguousarray(g.MomentaValues[0, min(1, cfg["numk"] - 1)])
+    u1 = np.ascontiguousarray(u1, dtype=np.int64)
+    u2 = np.ascontiguousarray(u2, dtype=np.int64)
+    t1, t2 = np.ascontiguousarray(t1, dtype=np.float64), np.ascontiguousarray(t2, dtype=np.float64)
+    vk = np.ascontiguousarray(vk, dtype=np.float64)
     rng = np.random.default_rng(0)
     P = np.zeros((Ns, Ns, 4), dtype=np.complex128, order="F")
     P[:, :, 0] = np.eye(Ns) * 0.5
@@ -332,56 +330,86 @@ def cpu_sample(cfg, n_max=2000):
     t0 = time.time()
     w, Z = fo.eigh_lower(H, iu)
     t_eig = time.time() - t0
+    del H
     t0 = time.time()
     occ = np.asfortranarray(np.conj(Z[:, :nl - 1]))
     Cb = blas.zherk(1.0, occ, lower=1)
     t_proj = time.time() - t0
+    del Cb, occ, Z
     t0 = time.time()
     out = np.zeros(2)
     lib.fo_energies_kf(C.c_int64(Ns), fo._ptr(X), fo._ptr(u1), fo._ptr(u2), fo._ptr(t1), fo._ptr(t2), C.byref(mdl),
                        fo._ptr(P), fo._ptr(out))
     t_en = time.time() - t0
-    del Cb
     f2, f3 = (N / Ns) ** 2, (N / Ns) ** 3
     parts = dict(assemble=t_asm * f2, zheevr=t_eig * f3, projector=t_proj * f3, energy=t_en * f2)
+    measured = dict(assemble=t_asm, zheevr=t_eig, projector=t_proj, energy=t_en)
     t_iter = so.Nk * (parts["assemble"] + parts["zheevr"] + parts["projector"]) + 3 * parts["energy"]
-    block = "" if Ns == N else (f" on the principal {Ns} x {Ns} block, scaled by (N/{Ns})^2 for the pair loops and "
-                                f"(N/{Ns})^3 for zheevr and the projector")
-    return dict(t_iter=t_iter, cores=cores, parts=parts,
-                sample=f"1 of {so.Nk} k points at N={N} (H(k) with ft/fv per pair, zheevr il=1..N/2+10, ZHERK bulk "
-                       f"projector; OpenMP/OpenBLAS on {cores} threads){block}; x {so.Nk} k + 3 energy passes")
+    if Ns == N:
+        how = (f"one full k point at N={N} (H(k) with ft/fv per pair, zheevr il=1..N/2+10, ZHERK bulk projector, "
+               f"one energy pass; OpenMP/OpenBLAS on {cores} threads), x {so.Nk} k + 3 energy passes")
+    else:
+        how = (f"one k point on the principal {Ns} x {Ns} block of the N={N} sites (H(k) with ft/fv per pair, "
+               f"zheevr il=1..{iu}, ZHERK projector, one energy pass; OpenMP/OpenBLAS on {cores} threads), "
+               f"EXTRAPOLATED to N by (N/{Ns})^2 for the pair loops and (N/{Ns})^3 for zheevr and the projector, "
+               f"x {so.Nk} k + 3 energy passes")
+    return dict(t_iter=t_iter, cores=cores, parts=parts, measured=measured, sample=how, full=(Ns == N))
+
+
+def run_reference(args, cfg):
+    """The reference arm: the oracle port (the reference's CPU algorithm restated; the Fortran
+    reference cannot be built here) on the host cores, one full-size k point, no GPU library."""
+    from oracle import forge_oracle as fo
+    so = fo.Setup(ntheta=cfg["ntheta"], numk=cfg["numk"], nfilling=cfg["nfilling"], epsilon=cfg["epsilon"])
+    t0 = time.time()
+    g = fo.build_geometry(so)
+    t_geo = time.time() - t0
+    tn = g.tn
+    cs = _cpu_k_point(fo, so, np.asarray(g.coords), g.ucell1, g.ucell2, tn[0], tn[1], g.vk(min(1, so.Nk - 1)),
+                      n_max=args.ref_n_max)
+    if cs is None:
+        return None
+    rec = PLAIN_FP64_RECORDED.get(cfg["name"])
+    iters = rec["iterations"] if rec else None
+    return dict(cs=cs, iters=iters, rec=rec, t_geo=t_geo)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=4, choices=sorted(CONFIGS))
     ap.add_argument("--mode", default="fast", choices=["fast", "mixed", "plain"],
-                    help="fast: learned warm start + mixed-precision iterations; mixed: plain guess + mixed; "
-                         "plain: plain guess + FP64")
-    ap.add_argument("--mixer", default="pulay", choices=["pulay", "oda"],
-                    help="SCF mixing of both modes: Anderson/Pulay or the reference's OptimalStep")
+                    help="fast: learned warm start + mixed-precision eigen-solve with eigenpair refinement; "
+                         "mixed: plain guess + the same; plain: plain guess + FP64")
+    ap.add_argument("--mixer", default="pulay", choices=["pulay", "oda"])
     ap.add_argument("--mix-depth", type=int, default=6)
     ap.add_argument("--mix-beta", type=float, default=0.7)
-    ap.add_argument("--degfactor", default="corrected", choices=["corrected", "reference"],
-                    help="occupation weight of the partially filled states (Setup degfactor_mode)")
+    ap.add_argument("--degfactor", default="corrected", choices=["corrected", "reference"])
     ap.add_argument("--tol", type=float, default=1e-6, help="mean-field residual (eV) that defines SCF")
-    ap.add_argument("--switch-tol", type=float, default=3e-6,
-                    help="fast/mixed modes: mixed -> FP64 below this residual (or when the mixed residual stalls)")
-    ap.add_argument("--itmax", type=int, default=60)
+    ap.add_argument("--itmax", type=int, default=40)
+    ap.add_argument("--budget-s", type=float, default=1200.0,
+                    help="wall-clock budget of the repo arm after which no further iteration starts")
     ap.add_argument("--converge", action="store_true",
-                    help="continue the SCF to --tol (minutes to hours at the headline workload) instead of "
-                         "taking the iteration counts from the recorded --converge run")
-    ap.add_argument("--e2e-steps", type=int, default=1)
+                    help="record run: continue to --tol within --itmax (no e2e, no CPU sample)")
+    ap.add_argument("--save-state", default="", help="npz path for the converged-state summary")
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--c3", action="store_true",
-                    help="C3-reduced solve (nenforceC3 = 1; the workload's numk must be a multiple of 3)")
+    ap.add_argument("--rr-width", type=int, default=32)
+    ap.add_argument("--ref-n-max", type=int, default=1 << 30,
+                    help="reference arm: largest principal block timed (default: the full N)")
+    ap.add_argument("--c3", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.converge:
+        # record run: no fixed K, the SCF stops at the tolerance (or itmax)
+        args.steps = 0
+        args.no_e2e = True
+        args.no_cpu_baseline = True
+        args.budget_s = max(args.budget_s, 1e9)
     cfg = dict(CONFIGS[args.config])
     if args.c3:
         if cfg["numk"] % 3:
@@ -389,30 +417,24 @@ def main():
         cfg["name"] += "_c3"
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
-    pg = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-        pg = dist
     if args.impl == "reference":
         if rank != 0:
             return
-        cs = cpu_sample(cfg)
-        if cs is None:
+        r = run_reference(args, cfg)
+        if r is None:
             print(json.dumps({"impl": "reference", "unavailable": "oracle C library not built"}))
             return
-        # the reference runs the plain FP64 SCF: as many iterations as the recorded plain run needed
-        rec_plain = _scf_record(cfg["name"], "plain", args.degfactor, args.mixer)
-        iters = int(rec_plain["n_fp64"]) if rec_plain else args.itmax
-        val = cs["t_iter"] * iters
+        cs = r["cs"]
+        val = cs["t_iter"] * r["iters"] if r["iters"] else None
         line = {"metric": METRIC, "value": val, "unit": "s", "n_gpus": 0, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": cs["t_iter"] * 1e3, "higher_is_better": False,
                 "impl": "reference", "dtype": "f64", "data": "synthetic",
-                "config": {"workload": cfg["name"], "iters": iters, "cpu_parts_s": cs["parts"],
-                           "iterations_source": (("ESTIMATED" if rec_plain.get("estimated") else "recorded")
-                                                 + f" plain FP64 iteration count with the {args.mixer} mixer "
-                                                 "(profiles/scf_records.json)") if rec_plain
-                           else "itmax (no recorded plain run)"},
+                "config": {"workload": cfg["name"], "iters": r["iters"], "cpu_parts_s": cs["parts"],
+                           "measured_s": cs["measured"], "geometry_s": r["t_geo"],
+                           "iterations_source": ("measured iteration count of the plain FP64 GPU SCF with the same "
+                                                 f"mixer ({r['rec']['command']}, {r['rec']['date']}); the "
+                                                 "time per iteration is this run's") if r["rec"] else
+                           "no plain FP64 record for this workload: value is null, ms_per_step is measured"},
                 "cpu_baseline": {"value": val, "unit": "s", "cores": cs["cores"], "kind": "port",
                                  "sample": cs["sample"]},
                 "e2e": {"value": val, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -421,76 +443,98 @@ def main():
         return
     if world > 1:
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0"))
-    r = run_ours(args, cfg, rank)
-    t_iter, t_scf, t_scf_e2e, e2e_iter = r["t_iter"], r["t_scf"], r["t_scf_e2e"], r["e2e_iter"]
-    if pg is not None:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    r = run_ours(args, cfg)
+    run = r["run"]
+    hist = run["hist"]
+    K = min(args.steps, len(hist))
+    timed = hist[:K]
+    step_ms = [h["ms"] for h in timed]
+    t_iter = float(np.mean(step_ms)) / 1e3 if step_ms else float("nan")
+    converged = run["t_conv"] is not None
+    t_scf = run["t_conv"] if converged else (hist[-1]["t_cum"] if hist else run["t_guess"])
+    iters = next((h["iter"] for h in hist if h["residual"] < args.tol), len(hist))
+    e2e = r["e2e"]
+    t_e2e = (e2e["t_conv"] if e2e and e2e["t_conv"] is not None else
+             (e2e["hist"][-1]["t_cum"] if e2e and e2e["hist"] else None))
+    if world > 1:
         import torch
-        t = torch.tensor([t_iter, t_scf, t_scf_e2e, e2e_iter], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_iter, t_scf, t_scf_e2e, e2e_iter = (float(x) for x in t)
+        import torch.distributed as dist
+        t = torch.tensor([t_iter, t_scf, t_e2e or 0.0], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_iter, t_scf = float(t[0]), float(t[1])
+        t_e2e = float(t[2]) if t_e2e is not None else None
     if rank != 0:
         return
     hbm, bf16, src = _peaks()
-    prof = r["prof"]
+    prof = run.get("prof", {})
     kernels = {k: v for k, v in prof.items() if v["launches"] > 0}
-    # the dominant kernel among those with a throughput roofline (the per-column latency-bound
-    # steps, bisection and inverse iteration have none)
-    roofed = {"assemble", "hemv", "her2k", "backtransform", "projector", "window", "energy", "lr_matvec", "mix"}
-    dom = max((k for k in kernels if k in roofed), key=lambda k: kernels[k]["ms"])
-    d = kernels[dom]
-    per_launch_ms = d["ms"] / d["launches"]
-    tensor_stages = {"her2k", "backtransform", "projector", "window", "refine"}
-    if args.mode != "plain" and dom in tensor_stages:
-        ach = d["flops"] / d["launches"] / (per_launch_ms * 1e-3) / 1e12
-        roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16}
-    else:
-        ach = d["bytes"] / d["launches"] / (per_launch_ms * 1e-3) / 1e9
-        roof = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm}
-    tr = _traffic(dom, d["bytes"] / d["launches"])
-    roof.update({"kernel": dom, "launches": d["launches"], "avg_launch_ms": per_launch_ms,
-                 "algorithmic_bytes_per_launch": d["bytes"] / d["launches"],
-                 "peak_source": src, "traffic": tr["bytes_per_launch"] if tr else None,
-                 "traffic_source": (f"{tr['source']}; ratio {tr['ratio_to_algorithmic']} x this run's algorithmic "
-                                    "bytes per launch") if tr else None})
-    iters = r["iters"]
-    line = {"metric": METRIC, "value": t_scf, "unit": "s", "n_gpus": world, "steps": args.steps,
+    roofed = {"assemble", "hemv", "her2k", "backtransform", "projector", "window", "energy", "lr_matvec", "mix",
+              "refine", "oa_gemm"}
+    roof = None
+    if any(k in roofed for k in kernels):
+        dom = max((k for k in kernels if k in roofed), key=lambda k: kernels[k]["ms"])
+        d = kernels[dom]
+        per_launch_ms = d["ms"] / d["launches"]
+        tensor_stages = {"her2k", "backtransform", "projector", "window", "oa_gemm"}
+        if args.mode != "plain" and dom in tensor_stages:
+            ach = d["flops"] / d["launches"] / (per_launch_ms * 1e-3) / 1e12
+            roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16}
+        else:
+            ach = d["bytes"] / d["launches"] / (per_launch_ms * 1e-3) / 1e9
+            roof = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm}
+        alg = d["bytes"] / d["launches"]
+        tr = NCU_TRAFFIC_RATIO.get(dom)
+        roof.update({"kernel": dom, "launches": d["launches"], "avg_launch_ms": per_launch_ms,
+                     "algorithmic_bytes_per_launch": alg, "algorithmic_flops_per_launch": d["flops"] / d["launches"],
+                     "peak_source": f"{src} (MEASURED_PEAKS.json)" if src == "measured" else src,
+                     "traffic": tr[0] * alg if tr else None,
+                     "traffic_source": f"{tr[1]}; ratio {tr[0]} x this run's algorithmic bytes per launch" if tr
+                     else None})
+    line = {"metric": METRIC, "value": t_scf, "unit": "s", "n_gpus": world, "steps": K,
             "warmup": args.warmup, "ms_per_step": t_iter * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.mode == "plain" else "f32+f64",
             "data": "synthetic",
             "config": {"workload": cfg["name"], "mode": args.mode, "degfactor": args.degfactor,
                        "mixer": f"{args.mixer}(depth={args.mix_depth},beta={args.mix_beta})" if args.mixer == "pulay"
-                       else "oda", "N": r["N"],
-                       "Nk": r["Nk"], "iters_to_scf": iters, "iters_mixed": r["n_mixed"], "iters_fp64": r["n_fp64"],
-                       "ms_per_iter": r["mean_by_prec"], "converged": r["converged"], "residual_tol_eV": args.tol,
-                       "final_residual": r["residual"], "iterations_source": r["source"],
-                       "setup_s": r["t_setup"], "guess_s": r["t_guess"], "parallelism": f"replicas{world}",
+                       else "oda", "N": r["N"], "Nk": r["Nk"], "converged": converged,
+                       "iters_to_scf": iters if converged else None, "iterations_run": len(hist),
+                       "residual_tol_eV": args.tol, "final_residual": hist[-1]["residual"] if hist else None,
+                       "residuals": [h["residual"] for h in hist],
+                       "energies": [h["TotalEnergy"] for h in hist],
+                       "guess_s": run["t_guess"], "setup_s": r["t_setup"], **run["guess_info"],
+                       "value_source": "CUDA events of this run: start of the guess to the end of the first "
+                                       "iteration below the residual tolerance",
+                       "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (H(k) batch >= 129 MB per step)"},
-            "e2e": {"value": t_scf_e2e, "unit": "s", "h2d_bytes_per_step": r["h2d"],
-                    "d2h_bytes_per_step": r["d2h"], "per_step_ms": e2e_iter * 1e3,
-                    "host_copy_overhead_ms_per_step": r["e2e_overhead_ms"]},
+            "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": e2e["h2d"] if e2e else 0,
+                    "d2h_bytes_per_step": e2e["d2h"] if e2e else 0,
+                    "converged": bool(e2e and e2e["t_conv"] is not None),
+                    "iterations": len(e2e["hist"]) if e2e else 0,
+                    "per_iter_s": e2e["per_iter_s"] if e2e else None} if e2e else None,
             "roofline": roof,
-            "gpu_launches": int(r["launches"]),
-            "stage_ms_per_step": {k: v["ms"] / max(1, args.steps) for k, v in kernels.items()},
-            "clocks": r["clocks"]}
-    if args.converge:
-        # the record that runs without --converge take their iteration counts from
-        line["record"] = {"n_mixed": r["n_mixed"], "n_fp64": r["n_fp64"], "converged": r["converged"],
-                          "ms_mixed": r["mean_by_prec"].get("mixed"), "ms_fp64": r["mean_by_prec"].get("fp64"),
-                          "final_residual": r["residual"],
-                          "residuals": [h["residual"] for h in r["hist"]],
-                          "precisions": [h["precision"] for h in r["hist"]],
-                          "energies": [h["TotalEnergy"] for h in r["hist"]]}
+            "gpu_launches": int(run.get("launches", 0)),
+            "stage_ms_per_step": {k: v["ms"] / max(1, K) for k, v in kernels.items()},
+            "clocks": r["clocks"],
+            "consistency": {"wall_s": r["wall_s"]}}
+    rec = PLAIN_FP64_RECORDED.get(cfg["name"])
+    if rec:
+        line["plain_fp64_recorded"] = rec
+    if args.save_state and r["state"] is not None:
+        np.savez_compressed(args.save_state, residuals=np.array([h["residual"] for h in hist]),
+                            energies=np.array([h["TotalEnergy"] for h in hist]),
+                            ms=np.array([h["ms"] for h in hist]), **r["state"])
     if not args.no_cpu_baseline and world == 1:
         cs = cpu_sample(cfg)
         if cs is not None:
-            # the CPU reference runs the plain SCF: the plain iteration count of the record
-            rec_plain = _scf_record(cfg["name"], "plain", args.degfactor, args.mixer)
-            n_plain = int(rec_plain["n_fp64"]) if rec_plain else iters
-            est = " (estimated count)" if rec_plain and rec_plain.get("estimated") else ""
-            line["cpu_baseline"] = {"value": cs["t_iter"] * n_plain, "unit": "s", "cores": cs["cores"],
-                                    "kind": "port", "iterations": n_plain,
-                                    "sample": cs["sample"] + f"; time-to-SCF = per-iteration time x {n_plain} "
-                                              f"plain-SCF iterations{est}"}
+            n_it = rec["iterations"] if rec else (iters if converged else None)
+            line["cpu_baseline"] = {"value": cs["t_iter"] * n_it if n_it else None, "unit": "s",
+                                    "cores": cs["cores"], "kind": "port", "iterations": n_it,
+                                    "ms_per_iteration": cs["t_iter"] * 1e3,
+                                    "sample": cs["sample"] + (f"; time-to-SCF = per-iteration time x {n_it} "
+                                                              "iterations of the plain FP64 record" if rec else
+                                                              f"; x {n_it} iterations of this run")}
     print(json.dumps(line))
 
 

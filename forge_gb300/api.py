@@ -121,6 +121,7 @@ SIGNATURES = {
     "forge_gpu_set_symmetry": [_P, _I, _I, _I, _P],
     "forge_gpu_set_valley": [_P, _I, _P],
     "forge_gpu_symmetrize": [_P, _P],
+    "forge_gpu_order_parameters": [_P, _P, _P, _P],
     "forge_host_sort_energies_2spins": [_I, _I, _P, _P, _P],
     "forge_host_fermi_2spins": [_P, _P, _P, _P, _P, _P, _P, _P],
 }
@@ -388,6 +389,16 @@ class HartreeFock:
         P = np.zeros(self._zfock_shape(), dtype=np.complex128, order="F") if copy_out else None
         _check(self.lib.forge_gpu_symmetrize(self.ctx, _ptr(P)))
         return P
+
+    def OrderParameters(self) -> dict:
+        """Order parameters of the current state P(0): layer and sublattice polarisation, C2T and C3
+        breaking norms (the oracle's order_parameters, evaluated on the device)."""
+        out = np.zeros(4)
+        c2 = _f(self.geometry.nC2pairs, np.int64)
+        c3 = _f(self.geometry.nC3pairs, np.int64)
+        _check(self.lib.forge_gpu_order_parameters(self.ctx, _ptr(c2), _ptr(c3), _ptr(out)))
+        return dict(layer_polarization=float(out[0]), sublattice_polarization=float(out[1]),
+                    c2t_breaking=float(out[2]), c3_breaking=float(out[3]))
 
     def set_mixing(self, mode: str = "oda", depth: int = 6, beta: float = 0.7):
         """SCF mixing: "oda" (the reference's OptimalStep) or "pulay" (Anderson / Pulay, `depth` steps)."""

@@ -729,6 +729,22 @@ int prepare_state_device(forge_ctx* x, double* Energies) {
     return 0;
 }
 
+// Anderson / Pulay mixing of (P_in, P_new) after the energy-forms pass of the pair: the residual,
+// the mixed state, its density, potential and energies
+int pulay_mix(forge_ctx* x) {
+    Context& c = x->c;
+    ScfScalars* sc = x->sc.as<ScfScalars>();
+    FORGE_TRY(scf_diis_residual(c, x->y.as<double>(), c.dens.as<double>(), x->dens_new.as<double>(),
+                                x->work.as<double>(), sc));
+    FORGE_TRY(pulay_step(x));
+    FORGE_TRY(scf_diis_dens(c, c.P.as<double2>(), c.dens.as<double>(), x->work.as<double>(), sc));
+    FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), c.P.as<double2>(), c.dens.as<double>(),
+                               c.dens.as<double>(), x->y.as<double>(), x->work.as<double>(), sc));
+    FORGE_TRY(scf_potential(c, x->y.as<double>(), c.dens.as<double>(), c.V.as<double>()));
+    FORGE_TRY(scf_oda(c, sc, 1));
+    return scf_diis_commit(c, sc);
+}
+
 }  // namespace
 
 extern "C" {
@@ -1044,6 +1060,56 @@ int forge_gpu_symmetrize(forge_ctx* x, double* zFock) {
         FORGE_CUDA(cudaMemcpyAsync(zFock, x->Pn.ptr, 4 * (size_t)c.N * c.N * sizeof(double2), cudaMemcpyDeviceToHost,
                                    c.stream));
     FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+int forge_gpu_order_parameters(forge_ctx* x, const int64_t* nC2pairs, const int64_t* nC3pairs, double* out) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!out) {
+        set_error(FORGE_ERR_ARG, "order_parameters: null output");
+        return FORGE_ERR_ARG;
+    }
+    const int64_t N = c.N;
+    // 0-based site maps; a map with a site left unpaired (0, as C2/C3_RelatedPoints leave it) is
+    // not used and its norm is NaN
+    std::vector<int64_t> maps(2 * N);
+    bool ok[2] = {nC2pairs != nullptr, nC3pairs != nullptr};
+    for (int t = 0; t < 2; ++t) {
+        const int64_t* src = t == 0 ? nC2pairs : nC3pairs;
+        for (int64_t i = 0; ok[t] && i < N; ++i) {
+            if (src[i] < 1 || src[i] > N) ok[t] = false;
+            else maps[t * N + i] = src[i] - 1;
+        }
+    }
+    const int nblocks = 2 * 152;
+    DevBuf dm, dpart;
+    FORGE_TRY(dm.ensure(2 * N * sizeof(int64_t)));
+    FORGE_TRY(dpart.ensure(nblocks * 4 * sizeof(double)));
+    FORGE_CUDA(cudaMemcpyAsync(dm.ptr, maps.data(), 2 * N * sizeof(int64_t), cudaMemcpyHostToDevice, c.stream));
+    const int64_t* m = dm.as<int64_t>();
+    int rc = launch_order_params(c.stream, c.P.as<double2>(), N, c.s.nlayers, ok[0] ? m : nullptr,
+                                 ok[1] ? m + N : nullptr, dpart.as<double>(), nblocks);
+    std::vector<double> part(nblocks * 4);
+    if (rc == 0) {
+        cudaError_t e = cudaMemcpyAsync(part.data(), dpart.ptr, part.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                        c.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+        if (e != cudaSuccess) {
+            set_error(FORGE_ERR_CUDA, "order_parameters: %s", cudaGetErrorString(e));
+            rc = FORGE_ERR_CUDA;
+        }
+    }
+    dm.release();
+    dpart.release();
+    if (rc) return rc;
+    double s[4] = {0, 0, 0, 0};
+    for (int b = 0; b < nblocks; ++b)
+        for (int t = 0; t < 4; ++t) s[t] += part[b * 4 + t];
+    out[0] = s[0];
+    out[1] = s[1];
+    out[2] = ok[0] ? std::sqrt(s[2]) : NAN;
+    out[3] = ok[1] ? std::sqrt(s[3]) : NAN;
     return 0;
 }
 
@@ -1503,11 +1569,17 @@ int forge_gpu_mix_potential(forge_ctx* x, double Step, double* DensityConvergenc
         return FORGE_ERR_STATE;
     }
     ScfScalars h;
-    FORGE_TRY(read_scalars(x, &h));
-    h.step = Step;
-    FORGE_TRY(write_scalars(x, &h));
-    FORGE_TRY(scf_mix(c, c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(), c.V.as<double>(),
-                      x->y.as<double>(), x->work.as<double>(), x->sc.as<ScfScalars>()));
+    if (x->mix_mode == FORGE_MIX_PULAY) {
+        // the Anderson / Pulay state replaces the OptimalStep mix (Step is not used); the energy
+        // forms of (P_in, P_new) come from forge_gpu_optimal_step
+        FORGE_TRY(pulay_mix(x));
+    } else {
+        FORGE_TRY(read_scalars(x, &h));
+        h.step = Step;
+        FORGE_TRY(write_scalars(x, &h));
+        FORGE_TRY(scf_mix(c, c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(), c.V.as<double>(),
+                          x->y.as<double>(), x->work.as<double>(), x->sc.as<ScfScalars>()));
+    }
     FORGE_TRY(read_scalars(x, &h));
     if (DensityConvergence) *DensityConvergence = h.dn_max;
     if (residual) *residual = h.residual;
@@ -1623,17 +1695,7 @@ int forge_gpu_scf_iteration(forge_ctx* x, double* Energies, forge_iter_report* r
                                x->dens_new.as<double>(), x->y.as<double>(), x->work.as<double>(),
                                x->sc.as<ScfScalars>()));
     if (x->mix_mode == FORGE_MIX_PULAY) {
-        // residual of (P_in, P_new), then the Anderson / Pulay state, its density, potential and energies
-        ScfScalars* sc = x->sc.as<ScfScalars>();
-        FORGE_TRY(scf_diis_residual(c, x->y.as<double>(), c.dens.as<double>(), x->dens_new.as<double>(),
-                                    x->work.as<double>(), sc));
-        FORGE_TRY(pulay_step(x));
-        FORGE_TRY(scf_diis_dens(c, c.P.as<double2>(), c.dens.as<double>(), x->work.as<double>(), sc));
-        FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), c.P.as<double2>(), c.dens.as<double>(),
-                                   c.dens.as<double>(), x->y.as<double>(), x->work.as<double>(), sc));
-        FORGE_TRY(scf_potential(c, x->y.as<double>(), c.dens.as<double>(), c.V.as<double>()));
-        FORGE_TRY(scf_oda(c, sc, 1));
-        FORGE_TRY(scf_diis_commit(c, sc));
+        FORGE_TRY(pulay_mix(x));
     } else {
         FORGE_TRY(scf_oda(c, x->sc.as<ScfScalars>(), 0));
         FORGE_TRY(scf_mix(c, c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(), c.V.as<double>(),

@@ -186,6 +186,9 @@ int rr_small(int n, const double2* G, const double2* S, double* theta, double2* 
 // symmetry switches of the SCF loop (symmetry.cu)
 int launch_symmetrize(cudaStream_t st, double2* P, double2* scratch, const int64_t* perm, int64_t N, bool T, bool C2,
                       bool C2T);
+// order parameters of P(0): nblocks x 4 partial sums (layer, sublattice, |P - C2T P|^2, |P - C3 P|^2)
+int launch_order_params(cudaStream_t st, const double2* P0, int64_t N, int64_t L, const int64_t* c2,
+                        const int64_t* c3, double* part, int nblocks);
 
 // device helpers shared across units
 __device__ double dev_ft(const forge_setup& s, double xi, double yi, double zi, double xj, double yj, double zj);

@@ -169,7 +169,10 @@ int forge_gpu_energies(forge_ctx* ctx, const double* zFock, double* KineticEnerg
 int forge_gpu_optimal_step(forge_ctx* ctx, double* Step, double* Energies);
 
 /* Main.f90:558-595: P = Step*P_new + (1-Step)*P_in, Density, DensityConvergence, Potential;
- * P_in <- P.  residual receives the mean-field residual (NULL allowed). */
+ * P_in <- P.  residual receives the mean-field residual (NULL allowed).  With FORGE_MIX_PULAY
+ * (forge_gpu_set_mixing) the new state is the Anderson / Pulay mix of the history instead and
+ * Step is not used; forge_gpu_optimal_step must still come first (its energy-forms pass of
+ * (P_in, P_new) feeds the Pulay residual), as in the reference's call order. */
 int forge_gpu_mix_potential(forge_ctx* ctx, double Step, double* DensityConvergence, double* residual);
 
 /* Initial guess without a checkpoint (Main.f90:236-346, nRead=0): non-interacting Solve,
@@ -234,6 +237,14 @@ int forge_gpu_set_symmetry(forge_ctx* ctx, int64_t nenforceT, int64_t nenforceC2
 /* The same averages on the device P_new of forge_gpu_get_fock, for hosts that call the routines one
  * by one; copies the result to zFock when it is not NULL. */
 int forge_gpu_symmetrize(forge_ctx* ctx, double* zFock);
+
+/* Order parameters of the current state P(R=0) (no counterpart in the reference, which computes
+ * none; defined from P and the site maps of C2_RelatedPoints / C3_RelatedPoints,
+ * Geometry.f90:1140-1223): out[0] layer polarisation sum_l (l - (L-1)/2) sum_{i in l} (n_i - 1/2),
+ * out[1] sublattice polarisation (A block minus B block of every layer), out[2] the C2T breaking
+ * norm ||P0(i,j) - P0(c2(j),c2(i))||_F, out[3] the C3 breaking norm ||P0(i,j) - P0(c3(i),c3(j))||_F.
+ * nC2pairs / nC3pairs are 1-based; a map that is NULL or leaves a site unpaired gives NaN. */
+int forge_gpu_order_parameters(forge_ctx* ctx, const int64_t* nC2pairs, const int64_t* nC3pairs, double* out);
 
 /* Selects FORGE_PREC_FP64 or FORGE_PREC_MIXED for subsequent solves. */
 int forge_gpu_set_precision(forge_ctx* ctx, int64_t precision);
