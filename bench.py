@@ -152,6 +152,9 @@ def _make(args, cfg):
     hf.set_mixing(args.mixer, args.mix_depth, args.mix_beta)
     if mixed:
         hf.set_refinement(args.rr_width)
+        if not args.no_oa:
+            # the eigenpair refinement once the SCF is within reach of the tolerance (latched)
+            hf.set_eigen_refinement(2, args.oa_below, 0.0, args.oa_depth)
     hf.LongRangeInteraction(copy_out=False)
     hf.synchronize()
     return S, hf
@@ -197,7 +200,8 @@ def scf_device(hf, S, args, n_steps, budget_s, t_start_wall, profile=False):
         t_cum = hf.elapsed_ms(0, slot) / 1e3
         prev = hist[-1]["t_cum"] if hist else t_guess
         rec = {"iter": i + 1, "ms": (t_cum - prev) * 1e3, "t_cum": t_cum, "residual": rep["residual"],
-               "TotalEnergy": rep["TotalEnergy"], "nPartOccStates": rep["nPartOccStates"], "info": info}
+               "TotalEnergy": rep["TotalEnergy"], "nPartOccStates": rep["nPartOccStates"], "info": info,
+               "refined": rep["refined"]}
         hist.append(rec)
         _log({k: (round(v, 1) if k == "ms" else v) for k, v in rec.items() if k != "t_cum"})
         if t_conv is None and rep["residual"] < args.tol:
@@ -398,6 +402,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rr-width", type=int, default=32)
+    ap.add_argument("--no-oa", action="store_true", help="mixed modes without the eigenpair refinement")
+    ap.add_argument("--oa-below", type=float, default=1e-3,
+                    help="mixed modes: residual (eV) below which every later solve is refined")
+    ap.add_argument("--oa-depth", type=int, default=4)
     ap.add_argument("--ref-n-max", type=int, default=1 << 30,
                     help="reference arm: largest principal block timed (default: the full N)")
     ap.add_argument("--c3", action="store_true")
@@ -502,6 +510,7 @@ def main():
                        "iters_to_scf": iters if converged else None, "iterations_run": len(hist),
                        "residual_tol_eV": args.tol, "final_residual": hist[-1]["residual"] if hist else None,
                        "residuals": [h["residual"] for h in hist],
+                       "refined": [h["refined"] for h in hist],
                        "energies": [h["TotalEnergy"] for h in hist],
                        "guess_s": run["t_guess"], "setup_s": r["t_setup"], **run["guess_info"],
                        "value_source": "CUDA events of this run: start of the guess to the end of the first "

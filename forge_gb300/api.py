@@ -44,7 +44,7 @@ class forge_iter_report(C.Structure):
         "Step", "DensityConvergence", "TotalEnergyIn", "TotalEnergy", "KineticEnergyIn", "FockEnergyIn",
         "HartreeEnergyIn", "HubbardEnergyIn", "KineticEnergy", "FockEnergy", "HartreeEnergy", "HubbardEnergy",
         "FermiEnergy", "DegFactor", "residual")] + [(n, C.c_int64) for n in (
-            "nFermiLevel", "nOccStates", "nPartOccStates", "info")]
+            "nFermiLevel", "nOccStates", "nPartOccStates", "info", "refined")]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -94,6 +94,7 @@ SIGNATURES = {
     "forge_gpu_set_precision": [_P, _I],
     "forge_gpu_set_mixing": [_P, _I, _I, C.c_double],
     "forge_gpu_set_refinement": [_P, _I],
+    "forge_gpu_set_eigen_refinement": [_P, _I, _D, _D, _I],
     "forge_selftest_rr_small": [_I, _P, _P, _P, _P],
     "forge_gpu_get_setup": [_P, _P],
     "forge_gpu_synchronize": [_P],
@@ -368,6 +369,11 @@ class HartreeFock:
         """FP64 Rayleigh-Ritz refinement of the top `width` bands after each mixed solve (0: off)."""
         _check(self.lib.forge_gpu_set_refinement(self.ctx, width))
 
+    def set_eigen_refinement(self, mode: int = 1, residual_below: float = 0.0, delta: float = 0.0, depth: int = 0):
+        """Eigenpair refinement of the mixed solve: 0 off, 1 every mixed solve, 2 once the SCF residual
+        is below residual_below (eV); delta (eV) and depth 0 = defaults (1e-3, 4)."""
+        _check(self.lib.forge_gpu_set_eigen_refinement(self.ctx, mode, residual_below, delta, depth))
+
     def set_c3(self, nenforceC3: int = 1):
         """nenforceC3 (Setup.f90:27): 1 = Solve_C3 / GetFock_C3, 0 = the full solve."""
         pairs = _f(self.geometry.nC3pairs, np.int64)
@@ -540,7 +546,7 @@ class HartreeFock:
         _check(self.lib.forge_gpu_synchronize(self.ctx))
 
     STAGES = ("tables", "long_range", "assemble", "trd_col", "hemv", "trd_finish", "her2k", "bisect", "invit",
-              "backtransform", "projector", "window", "sort", "energy", "lr_matvec", "mix", "refine")
+              "backtransform", "projector", "window", "sort", "energy", "lr_matvec", "mix", "refine", "oa_gemm", "oa")
 
     def mark(self, slot: int):
         """Records a CUDA event in `slot` on the context's stream."""

@@ -78,6 +78,11 @@ size_t eig_mixed_workspace_bytes(int64_t n, int64_t iu, int64_t batch);
 int rr_window(cudaStream_t st, const double2* H, int64_t strideH, double2* X, int64_t ldx, int64_t strideX, double* w,
               int64_t iu, int64_t n, int64_t c0, int64_t nw, int64_t batch, void* ws);
 size_t rr_window_workspace_bytes(int64_t n, int64_t batch);
+const float* eig_mixed_planes(void* mixed_ws, int64_t n, int64_t iu, int64_t batch, int64_t* n4);
+size_t oa_workspace_bytes(int64_t n, int64_t iu);
+int oa_refine(cudaStream_t st, double2* H, int64_t strideH, const float* Xs, int64_t n4, int64_t nall,
+              const double* lam, int64_t n, int64_t iu, int64_t batch, double2* X, int64_t ldx, int64_t strideX,
+              double* w_out, int64_t w_stride, void* ws, int* err, double delta, int depth);
 
 }  // namespace forge
 
@@ -95,6 +100,14 @@ struct forge_ctx {
     DevBuf rrws;           // FP64 window refinement of the mixed path
     DevBuf pstates;        // partially occupied states of the fused projector
     int64_t rr_width = 32; // bands refined in FP64 after each mixed solve (0: off)
+    // eigenpair refinement of the mixed solve (forge_gpu_set_eigen_refinement): mode 0 off, 1 every
+    // mixed solve, 2 once the last SCF residual is below oa_below
+    int oa_mode = 0;
+    double oa_below = 0.0, oa_delta = 1e-3;
+    int oa_depth = 4;
+    bool oa_active = false, oa_latched = false;
+    double last_residual = INFINITY;
+    DevBuf oaws, w_all;
     int64_t eig_batch = 0;
     int64_t k_begin = 0, k_end = 0;  // local k range (k_end = 0: all k)
     // mixing: FORGE_MIX_ODA (OptimalStep, the reference) or FORGE_MIX_PULAY (Anderson / Pulay)
@@ -139,14 +152,18 @@ int check_ctx(forge_ctx* x) {
 int choose_batch(forge_ctx* x) {
     Context& c = x->c;
     const int64_t N = c.N, iu = c.nUpper;
-    size_t per_k = (size_t)N * N * 16 + eig_workspace_bytes(N, iu, 1);
-    if (c.precision == FORGE_PREC_MIXED) per_k += eig_mixed_workspace_bytes(N, iu, 1);
+    const bool oa = c.precision == FORGE_PREC_MIXED && x->oa_mode != 0;
+    const int64_t iu_solve = oa ? N : iu;   // the refinement needs every eigenpair of the mixed solve
+    size_t per_k = (size_t)N * N * 16 + eig_workspace_bytes(N, iu_solve, 1);
+    if (c.precision == FORGE_PREC_MIXED) per_k += eig_mixed_workspace_bytes(N, iu_solve, 1);
+    if (oa) per_k += (size_t)N * 8;
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
     // kept free: 8 GB headroom, the eigenvectors of every k, the four bulk cells and the
     // projector / window work arrays allocated after the batch is chosen
     const int64_t xslots = x->c3 ? x->c3t.nslots + (int64_t)x->c3t.reps.size() : c.Nk;
-    const size_t reserve = ((size_t)8 << 30) + (size_t)xslots * N * iu * 16 + (size_t)10 * N * N * 16;
+    const size_t reserve = ((size_t)8 << 30) + (size_t)xslots * N * iu * 16 + (size_t)10 * N * N * 16 +
+                           (oa ? oa_workspace_bytes(N, iu) : 0);
     const size_t budget = freeb > reserve ? freeb - reserve : freeb / 4;
     int64_t b = (int64_t)(budget / per_k);
     // FORGE_EIG_BATCH caps the number of k points solved per launch (memory control)
@@ -178,8 +195,15 @@ int ensure_solve_buffers(forge_ctx* x) {
         FORGE_TRY(x->c3_Xr.ensure(nr * N * iu * sizeof(double2)));
         FORGE_TRY(x->c3_wr.ensure(nr * iu * sizeof(double)));
     }
-    FORGE_TRY(x->eigws.ensure(eig_workspace_bytes(N, iu, B)));
-    if (c.precision == FORGE_PREC_MIXED) FORGE_TRY(x->mixws.ensure(eig_mixed_workspace_bytes(N, iu, B)));
+    const bool oa = c.precision == FORGE_PREC_MIXED && x->oa_mode != 0;
+    const int64_t iu_solve = oa ? N : iu;
+    FORGE_TRY(x->eigws.ensure(eig_workspace_bytes(N, iu_solve, B)));
+    if (c.precision == FORGE_PREC_MIXED) FORGE_TRY(x->mixws.ensure(eig_mixed_workspace_bytes(N, iu_solve, B)));
+    if (oa) {
+        FORGE_TRY(x->w_all.ensure((size_t)B * N * sizeof(double)));
+        FORGE_TRY(x->oaws.ensure(oa_workspace_bytes(N, iu)));
+        FORGE_TRY(x->tcerr.ensure(sizeof(int)));
+    }
     FORGE_TRY(c.bulk.ensure(4 * NN * sizeof(double2)));
     return 0;
 }
@@ -212,16 +236,46 @@ int eig_batch_run(forge_ctx* x, int64_t k0, int64_t nb, int* info, double2* Xdst
     g.strideX = N * iu;
     g.w = wdst ? wdst : x->w.as<double>() + (size_t)k0 * iu;
     g.ortol_rel = 1e-7;
+    const bool oa = c.precision == FORGE_PREC_MIXED && x->oa_active;
+    double* w_iu = g.w;
+    if (oa) {
+        // every eigenpair of the mixed solve; FP64 columns 1..iu, eigenvalues of all N in w_all
+        g.iu = N;
+        g.iu_out = iu;
+        g.w = x->w_all.as<double>();
+    }
     eig_bind_workspace(g, x->eigws.ptr);
     if (c.precision == FORGE_PREC_MIXED) {
-        int rc = eig_mixed(c.stream, g, x->mixws.ptr);
+        auto solve = [&]() -> int {
+            int r = eig_mixed(c.stream, g, x->mixws.ptr);
+            if (r || !oa) return r;
+            // FP64-accurate eigenpairs 1..iu from the mixed ones (tensor-core refinement)
+            int64_t n4 = 0;
+            const float* planes = eig_mixed_planes(x->mixws.ptr, N, N, nb, &n4);
+            FORGE_CUDA(cudaMemsetAsync(x->tcerr.ptr, 0, sizeof(int), c.stream));
+            r = oa_refine(c.stream, g.A, g.strideA, planes, n4, N, g.w, N, iu, nb, g.X, g.ldx, g.strideX, w_iu, iu,
+                          x->oaws.ptr, x->tcerr.as<int>(), x->oa_delta, x->oa_depth);
+            if (r) return r;
+            int herr = 0;
+            FORGE_CUDA(cudaMemcpyAsync(&herr, x->tcerr.ptr, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+            FORGE_CUDA(cudaStreamSynchronize(c.stream));
+            if (herr) {
+                set_error(FORGE_ERR_TIMEOUT, "tcgen05 GEMM of the eigenpair refinement: a bounded mbarrier wait gave up");
+                return FORGE_ERR_TIMEOUT;
+            }
+            return 0;
+        };
+        int rc = solve();
         if (rc == FORGE_ERR_TIMEOUT) {
             // a bounded tensor-core wait gave up (the kernel drained and freed its TMEM): the
-            // input H(k) is untouched, so the batch is solved again once
+            // input H(k) is unchanged (the refinement only mirrors its lower triangle), so the
+            // batch is solved again once
             std::fprintf(stderr, "forge: %s; solving the batch again\n", forge_gpu_last_error());
-            rc = eig_mixed(c.stream, g, x->mixws.ptr);
+            rc = solve();
         }
         FORGE_TRY(rc);
+        g.w = w_iu;
+        g.iu = iu;
         if (x->rr_width > 0) {
             // FP64 Rayleigh-Ritz on the top rr_width computed bands (the window around the Fermi level)
             const int64_t nw = std::min<int64_t>(x->rr_width, iu);
@@ -293,6 +347,10 @@ void expand_c3_states(forge_ctx* x, std::vector<WinState>& st) {
 // 1..nLower-1 (not divided by Nk), as Solve returns it
 int solve_device(forge_ctx* x, int* info, bool with_projector = true) {
     Context& c = x->c;
+    // mode 2 latches: once an SCF residual fell below oa_below, every later solve of that SCF
+    // (until the next guess or state load) is refined
+    if (x->oa_mode == 2 && x->last_residual < x->oa_below) x->oa_latched = true;
+    x->oa_active = c.precision == FORGE_PREC_MIXED && (x->oa_mode == 1 || (x->oa_mode == 2 && x->oa_latched));
     FORGE_TRY(ensure_solve_buffers(x));
     const int64_t N = c.N, Nk = c.Nk, B = x->eig_batch;
     const size_t NN = (size_t)N * N;
@@ -886,7 +944,7 @@ int forge_gpu_finalize(forge_ctx* x) {
                       &x->projws, &x->tcerr, &x->diis_hist, &x->diis_rprev, &x->diis_part, &x->rrws, &x->pstates,
                       &x->c3_Xr, &x->c3_wr, &x->c3_tab, &x->c3_perm, &x->c3_phase, &x->c2_perm,
                       &x->v_rowp, &x->v_col, &x->v_coef, &x->v_code, &x->v_ph, &x->v_W, &x->v_G, &x->v_S,
-                      &x->v_Xv, &x->v_st};
+                      &x->v_Xv, &x->v_st, &x->oaws, &x->w_all};
     for (DevBuf* b : bufs) b->release();
     if (c.stream) cudaStreamDestroy(c.stream);
     delete x;
@@ -914,6 +972,20 @@ int forge_gpu_set_refinement(forge_ctx* x, int64_t width) {
         return FORGE_ERR_ARG;
     }
     x->rr_width = width;
+    return 0;
+}
+
+int forge_gpu_set_eigen_refinement(forge_ctx* x, int64_t mode, double residual_below, double delta, int64_t depth) {
+    FORGE_TRY(check_ctx(x));
+    if (mode < 0 || mode > 2 || depth < 0 || depth > 4 || !(residual_below >= 0.0) || !(delta >= 0.0)) {
+        set_error(FORGE_ERR_ARG, "set_eigen_refinement: mode 0..2, depth 0..4, residual_below >= 0, delta >= 0");
+        return FORGE_ERR_ARG;
+    }
+    if ((x->oa_mode != 0) != (mode != 0)) x->eig_batch = 0;   // the solve's memory per k changes
+    x->oa_mode = (int)mode;
+    x->oa_below = residual_below;
+    x->oa_delta = delta > 0.0 ? delta : 1e-3;
+    x->oa_depth = depth > 0 ? (int)depth : 4;
     return 0;
 }
 
@@ -1207,6 +1279,8 @@ int forge_gpu_long_range(forge_ctx* x, double* LongRange) {
 int forge_gpu_set_state(forge_ctx* x, const double* zFock) {
     FORGE_TRY(check_ctx(x));
     diis_reset(x);
+    x->last_residual = INFINITY;
+    x->oa_latched = false;
     if (!zFock) {
         set_error(FORGE_ERR_ARG, "forge_gpu_set_state: null zFock");
         return FORGE_ERR_ARG;
@@ -1264,12 +1338,17 @@ int forge_gpu_zheevr_batch(forge_ctx* x, int64_t nb, const double* A, int64_t iu
         return FORGE_ERR_ARG;
     }
     const size_t NN = (size_t)N * N;
-    DevBuf dA, dX, dw, ws, mws;
+    const bool oa = c.precision == FORGE_PREC_MIXED && x->oa_mode != 0;
+    const int64_t iu_solve = oa ? N : iu;
+    DevBuf dA, dX, dw, ws, mws, wall, ows, oerr;
     int rc = 0;
     if ((rc = dA.ensure(nb * NN * sizeof(double2))) || (rc = dX.ensure(nb * N * iu * sizeof(double2))) ||
-        (rc = dw.ensure(nb * iu * sizeof(double))) || (rc = ws.ensure(eig_workspace_bytes(N, iu, nb))))
+        (rc = dw.ensure(nb * iu * sizeof(double))) || (rc = ws.ensure(eig_workspace_bytes(N, iu_solve, nb))))
         return rc;
-    if (c.precision == FORGE_PREC_MIXED && (rc = mws.ensure(eig_mixed_workspace_bytes(N, iu, nb)))) return rc;
+    if (c.precision == FORGE_PREC_MIXED && (rc = mws.ensure(eig_mixed_workspace_bytes(N, iu_solve, nb)))) return rc;
+    if (oa && ((rc = wall.ensure(nb * N * sizeof(double))) || (rc = ows.ensure(oa_workspace_bytes(N, iu))) ||
+               (rc = oerr.ensure(sizeof(int)))))
+        return rc;
     FORGE_CUDA(cudaMemcpyAsync(dA.ptr, A, nb * NN * sizeof(double2), cudaMemcpyHostToDevice, c.stream));
     EigArgs g{};
     g.n = N;
@@ -1283,8 +1362,28 @@ int forge_gpu_zheevr_batch(forge_ctx* x, int64_t nb, const double* A, int64_t iu
     g.strideX = N * iu;
     g.w = dw.as<double>();
     g.ortol_rel = 1e-7;
+    if (oa) {
+        g.iu = N;
+        g.iu_out = iu;
+        g.w = wall.as<double>();
+    }
     eig_bind_workspace(g, ws.ptr);
     rc = (c.precision == FORGE_PREC_MIXED) ? eig_mixed(c.stream, g, mws.ptr) : eig_fp64(c.stream, g);
+    if (!rc && oa) {
+        int64_t n4 = 0;
+        const float* planes = eig_mixed_planes(mws.ptr, N, N, nb, &n4);
+        cudaMemsetAsync(oerr.ptr, 0, sizeof(int), c.stream);
+        rc = oa_refine(c.stream, g.A, g.strideA, planes, n4, N, g.w, N, iu, nb, g.X, g.ldx, g.strideX, dw.as<double>(),
+                       iu, ows.ptr, oerr.as<int>(), x->oa_delta, x->oa_depth);
+        int herr = 0;
+        if (!rc && (cudaMemcpyAsync(&herr, oerr.ptr, sizeof(int), cudaMemcpyDeviceToHost, c.stream) != cudaSuccess ||
+                    cudaStreamSynchronize(c.stream) != cudaSuccess || herr)) {
+            set_error(FORGE_ERR_TIMEOUT, "eigenpair refinement: tensor-core wait gave up or CUDA error");
+            rc = FORGE_ERR_TIMEOUT;
+        }
+        g.w = dw.as<double>();
+        g.iu = iu;
+    }
     DevBuf rws;
     if (!rc && c.precision == FORGE_PREC_MIXED && x->rr_width > 0) {
         // the same FP64 window refinement as the SCF's solves
@@ -1305,6 +1404,9 @@ int forge_gpu_zheevr_batch(forge_ctx* x, int64_t nb, const double* A, int64_t iu
     dw.release();
     ws.release();
     mws.release();
+    wall.release();
+    ows.release();
+    oerr.release();
     if (rc) return rc;
     int bad = 0;
     for (int64_t b = 0; b < nb; ++b) bad += fails[b] ? 1 : 0;
@@ -1583,6 +1685,7 @@ int forge_gpu_mix_potential(forge_ctx* x, double Step, double* DensityConvergenc
     FORGE_TRY(read_scalars(x, &h));
     if (DensityConvergence) *DensityConvergence = h.dn_max;
     if (residual) *residual = h.residual;
+    x->last_residual = h.residual;
     x->have_pnew = false;
     return 0;
 }
@@ -1590,6 +1693,8 @@ int forge_gpu_mix_potential(forge_ctx* x, double Step, double* DensityConvergenc
 int forge_gpu_plain_guess(forge_ctx* x, double* Energies) {
     FORGE_TRY(check_ctx(x));
     diis_reset(x);
+    x->last_residual = INFINITY;
+    x->oa_latched = false;
     Context& c = x->c;
     if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
     const size_t NN = (size_t)c.N * c.N;
@@ -1609,6 +1714,8 @@ int forge_gpu_plain_guess(forge_ctx* x, double* Energies) {
 int forge_gpu_field_guess(forge_ctx* x, const double* zFock, double* Energies, double* residuals) {
     FORGE_TRY(check_ctx(x));
     diis_reset(x);
+    x->last_residual = INFINITY;
+    x->oa_latched = false;
     Context& c = x->c;
     if (!zFock || !residuals) {
         set_error(FORGE_ERR_ARG, "field_guess: null argument");
@@ -1664,6 +1771,8 @@ int forge_gpu_field_guess(forge_ctx* x, const double* zFock, double* Energies, d
 int forge_gpu_prepare_state(forge_ctx* x, double* Energies) {
     FORGE_TRY(check_ctx(x));
     diis_reset(x);
+    x->last_residual = INFINITY;
+    x->oa_latched = false;
     Context& c = x->c;
     if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
     return prepare_state_device(x, Energies);
@@ -1703,9 +1812,11 @@ int forge_gpu_scf_iteration(forge_ctx* x, double* Energies, forge_iter_report* r
     }
     FORGE_TRY(read_scalars(x, &h));
     x->have_pnew = false;
+    x->last_residual = h.residual;
     if (Energies)
         for (int t = 0; t < 4; ++t) Energies[t] = h.Eout[t];
     if (rep) {
+        rep->refined = x->oa_active ? 1 : 0;
         rep->Step = h.step;
         rep->DensityConvergence = h.dn_max;
         rep->TotalEnergyIn = h.Etot_in;

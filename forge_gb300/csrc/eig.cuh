@@ -37,6 +37,7 @@ struct EigArgs {
     float* tf;                  // batch x 2n: FP32 copies of d and e^2 (FP32 bisection)
     double ortol_rel;
     int bisect_f32 = 0;         // 1: FP32 bisection first, FP64 bisection from its bracket
+    int64_t iu_out = 0;         // mixed solver: FP64 columns written to X (0: all iu)
 };
 
 // workspace sizes (bytes) for a given problem

@@ -103,6 +103,19 @@ void carve(MixedWs& w, Carve& c) {
 }
 }  // namespace
 
+// the TF32 hi / lo eigenvector planes of the last eig_mixed call on this workspace (four planes of
+// n4 x iu floats per matrix: hi.re, hi.im, lo.re, lo.im, column-major)
+const float* eig_mixed_planes(void* mixed_ws, int64_t n, int64_t iu, int64_t batch, int64_t* n4) {
+    MixedWs w{};
+    w.n = n;
+    w.iu = iu;
+    w.B = batch;
+    Carve c{static_cast<char*>(mixed_ws)};
+    carve(w, c);
+    *n4 = w.n4;
+    return w.Xs;
+}
+
 size_t eig_mixed_workspace_bytes(int64_t n, int64_t iu, int64_t batch) {
     MixedWs w{};
     w.n = n;
@@ -148,12 +161,12 @@ __global__ void k_z_to_planes(const double* __restrict__ Z, int64_t n, int64_t n
     }
 }
 
-__global__ void k_planes_to_x(const float* __restrict__ Xs, int64_t n, int64_t n4, int64_t iu,
+__global__ void k_planes_to_x(const float* __restrict__ Xs, int64_t n, int64_t n4, int64_t iu, int64_t ncols,
                               double2* __restrict__ X, int64_t ldx, int64_t strideX) {
     const int64_t b = blockIdx.y;
     const size_t P = (size_t)n4 * iu;
     const float* S = Xs + b * 4 * P;
-    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < (size_t)n * iu;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < (size_t)n * ncols;
          q += (size_t)gridDim.x * blockDim.x) {
         const int64_t c = q / n, r = q - c * n;
         const size_t o = (size_t)c * n4 + r;
@@ -608,9 +621,11 @@ int eig_mixed(cudaStream_t st, EigArgs& g, void* mixed_ws) {
     prof_begin(ST_BACKTRANSFORM);
     FORGE_TRY(backtransform_tc(st, ws, batch));
     prof_end(ST_BACKTRANSFORM, batch * (double)n * iu * 16.0 * 2.0, batch * 3.0 * 8.0 * (double)n * n * iu);
-    k_planes_to_x<<<dim3(1216, (unsigned)batch), 256, 0, st>>>(ws.Xs, n, ws.n4, iu, g.X, g.ldx, g.strideX);
+    // FP64 copies of the first iu_out columns (the planes keep all iu for the eigenpair refinement)
+    const int64_t iu_out = (g.iu_out > 0 && g.iu_out < iu) ? g.iu_out : iu;
+    k_planes_to_x<<<dim3(1216, (unsigned)batch), 256, 0, st>>>(ws.Xs, n, ws.n4, iu, iu_out, g.X, g.ldx, g.strideX);
     FORGE_LAUNCH_CHECK();
-    k_normalize_cols<<<dim3((unsigned)iu, (unsigned)batch), 256, 0, st>>>(g.X, n, iu, g.ldx, g.strideX);
+    k_normalize_cols<<<dim3((unsigned)iu_out, (unsigned)batch), 256, 0, st>>>(g.X, n, iu_out, g.ldx, g.strideX);
     FORGE_LAUNCH_CHECK();
     int herr = 0;
     FORGE_CUDA(cudaMemcpyAsync(&herr, ws.err, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -2,8 +2,7 @@
 // LapackRoutines.f90:381-433, for one matrix).
 //
 // Some callers cannot allocate device memory at call time: code running inside a memory
-// pool or arena that owns every byte of the GPU, real-time loops where cudaMalloc /
-// cudaFree would stall or synchronise the device, and hosts that manage all device buffers
+// pool or arena that owns every byte of the GPU, and hosts that manage all device buffers
 // themselves and hand this library only pointers.  forge_gpu_zheevr_noalloc serves them: the
 // caller passes device pointers for its input and outputs and a stream, and the solver's
 // workspace lives in the file-scope device array below, sized for matrices up to
@@ -15,8 +14,13 @@
 // each call.  Calls whose work overlaps on the GPU race on the array, so callers must order
 // them (one stream, or events).  Host code only uses the array through the device address
 // obtained with cudaGetSymbolAddress, once per device with that device current, during the
-// first call on that device: make that first call before any stream capture begins.
+// first call on that device (std::call_once per device: concurrent first calls from several
+// host threads look it up once).  Each call synchronises its stream at the end to read the
+// solver's convergence flag, so it blocks the host and cannot be recorded into a CUDA graph.
+// The call hides its work from the calling thread's context profiler (a thread-local pointer)
+// for its duration, since profiling would create events.
 #include <cstring>
+#include <mutex>
 
 #include "eig.cuh"
 
@@ -27,8 +31,10 @@ constexpr size_t kNoAllocBytes = FORGE_NOALLOC_SCRATCH_BYTES;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-// device address of g_noalloc_scratch per device (0 = not set up yet)
+// device address of g_noalloc_scratch per device, looked up once per device
 static void* g_noalloc_ptr[64] = {};
+static cudaError_t g_noalloc_err[64] = {};
+static std::once_flag g_noalloc_once[64];
 
 }  // namespace forge
 
@@ -56,10 +62,15 @@ extern "C" int forge_gpu_zheevr_noalloc(double* A, int64_t n, int64_t iu, double
         set_error(FORGE_ERR_ARG, "zheevr_noalloc: device ordinal %d out of range", dev);
         return FORGE_ERR_ARG;
     }
-    if (!g_noalloc_ptr[dev]) {
+    std::call_once(g_noalloc_once[dev], [dev]() {
         void* p = nullptr;
-        FORGE_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_err[dev] = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         g_noalloc_ptr[dev] = p;
+    });
+    if (g_noalloc_err[dev] != cudaSuccess || !g_noalloc_ptr[dev]) {
+        set_error(FORGE_ERR_CUDA, "zheevr_noalloc: cudaGetSymbolAddress of the static workspace failed: %s",
+                  cudaGetErrorString(g_noalloc_err[dev]));
+        return FORGE_ERR_CUDA;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // no context profiler records into this call (it would create events)

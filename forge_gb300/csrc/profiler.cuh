@@ -29,6 +29,8 @@ enum ProfStage {
     ST_LRMATVEC,
     ST_MIX,
     ST_REFINE,
+    ST_OA_GEMM,   // sliced (error-free) residual product H X of the eigenpair refinement
+    ST_OA,        // the refinement's other steps: slices, overlaps, correction, update
     ST_COUNT
 };
 

@@ -16,6 +16,14 @@
 //
 // Complex products run as real GEMMs over operands staged by the callers (real/imag planes,
 // and hi/lo TF32 splits for FP32-accurate results: a*b ~ ah*bh + ah*bl + al*bh).
+//
+// Exact-block mode (FLUSH > 1, DF = true; the sliced products of the eigenpair refinement):
+// the operands are integer slices |s| <= 256 (Ozaki et al., "Error-free transformations of
+// matrix multiplication by using fast routines of matrix multiplication and its applications",
+// Numer. Algorithms 59, 2012), so a K block of FLUSH x 32 <= 256 products sums to an integer
+// below 2^24 and TMEM holds it exactly.  Each such block is scaled by 2^-sexp[segment] (exact)
+// and added into double-float (hi, lo) registers with an error-free TwoSum; the epilogue gets
+// hi + lo as doubles.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -45,9 +53,11 @@ struct TcOperand {
 // K-block -> TMA coordinate map of one operand.  The GEMM's K runs over nseg segments of
 // nkp blocks of 32; segment s reads plane zsel[s] (+ zbatch * batch index) starting at
 // element koff of each row.  A plain operand is nseg = 1, zsel = {0}, zbatch = 1.
+constexpr int TC_MAXSEG = 32;
 struct TcKMap {
     int32_t nkp, nseg, koff, zbatch;
-    int32_t zsel[8];
+    int32_t zsel[TC_MAXSEG];
+    int8_t sexp[TC_MAXSEG];   // exact-block mode: segment s is scaled by 2^-sexp[s] (A map)
 };
 
 __host__ __device__ inline TcKMap tc_kmap_plain(int64_t K) {
@@ -150,11 +160,11 @@ __device__ inline void tmem_ld32(uint32_t taddr, float* v) {
     for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
 }
 
-template <class EPI>
-__global__ void __launch_bounds__(TC_THREADS, 2)
+template <class EPI, int FLUSH = 1, bool DF = false>
+__global__ void __launch_bounds__(TC_THREADS, DF ? 1 : 2)
     k_tc_gemm_tf32(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int64_t M,
-                   int64_t N, TcKMap ka, TcKMap kb_map, int64_t lower_div, int32_t ksplit, int32_t kchunk, EPI epi,
-                   int* err) {
+                   int64_t N, const __grid_constant__ TcKMap ka, const __grid_constant__ TcKMap kb_map,
+                   int64_t lower_div, int32_t ksplit, int32_t kchunk, EPI epi, int* err) {
     // lower_div > 0: skip tiles whose rows (divided by lower_div) all lie above the diagonal
     if (lower_div > 0 && ((int64_t)blockIdx.x * TC_BM + TC_BM - 1) / lower_div < (int64_t)blockIdx.y * TC_BN) return;
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
@@ -229,17 +239,20 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            // ---- MMA issuer: K block kb accumulates alone into TMEM buffer kb & 1
+            // ---- MMA issuer: each group of FLUSH K blocks accumulates alone into TMEM buffer
+            // (group & 1)
             const uint32_t idesc = tc_idesc_tf32();
             for (int kb = 0; kb < nk; ++kb) {
                 const int s = kb % TC_STAGES;
                 const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
-                const int buf = kb & 1, use = kb >> 1;
+                const int grp = kb / FLUSH, buf = grp & 1, use = grp >> 1;
+                const bool first = (kb % FLUSH) == 0;
+                const bool last = (kb % FLUSH) == FLUSH - 1 || kb == nk - 1;
                 if (!mbar_wait(&full[s], ph, abort_flag)) {
                     *abort_flag = 1;
                     break;
                 }
-                if (use > 0 && !mbar_wait(&tfree[buf], (uint32_t)(use - 1) & 1u, abort_flag)) {
+                if (first && use > 0 && !mbar_wait(&tfree[buf], (uint32_t)(use - 1) & 1u, abort_flag)) {
                     *abort_flag = 1;
                     break;
                 }
@@ -249,10 +262,10 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
                 for (int kk = 0; kk < TC_BK / 8; ++kk) {
                     // K = 8 tf32 = 32 bytes per MMA: advance the start address inside the 128B swizzle atom
                     tc_mma_tf32(tmem + (uint32_t)(buf * TC_BN), umma_desc_sw128(a0 + kk * 32),
-                                umma_desc_sw128(b0 + kk * 32), idesc, kk > 0 ? 1u : 0u);
+                                umma_desc_sw128(b0 + kk * 32), idesc, (!first || kk > 0) ? 1u : 0u);
                 }
-                tc_commit(&empty[s]);   // frees the stage once these MMAs have read it
-                tc_commit(&tfull[buf]);  // the block's partial product is in TMEM
+                tc_commit(&empty[s]);              // frees the stage once these MMAs have read it
+                if (last) tc_commit(&tfull[buf]);  // the group's partial product is in TMEM
                 *n_consumed = kb + 1;
             }
             // arrives once every MMA issued above has completed (immediately if none was issued)
@@ -264,23 +277,44 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
         const int64_t row = m0 + quarter * 32 + lane;
         const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16);
         float acc[TC_BN];
+        float lo[DF ? TC_BN : 1];
 #pragma unroll
         for (int q = 0; q < TC_BN; ++q) acc[q] = 0.f;
+        if constexpr (DF) {
+#pragma unroll
+            for (int q = 0; q < TC_BN; ++q) lo[q] = 0.f;
+        }
         bool ok = true;
-        for (int kb = 0; kb < nk; ++kb) {
-            const int buf = kb & 1, use = kb >> 1;
+        const int ngrp = (nk + FLUSH - 1) / FLUSH;
+        for (int grp = 0; grp < ngrp; ++grp) {
+            const int buf = grp & 1, use = grp >> 1;
             if (!mbar_wait_warp(&tfull[buf], (uint32_t)use & 1u, abort_flag)) {
                 ok = false;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            float scl = 1.f;
+            // 2^-sexp (0 <= sexp <= 100) built from its exponent bits: exact
+            if constexpr (DF) scl = __int_as_float((127 - (int)ka.sexp[(kb_lo + grp * FLUSH) / ka.nkp]) << 23);
 #pragma unroll
             for (int h = 0; h < TC_BN; h += 32) {
                 float v[32];
                 tmem_ld32(trow + (uint32_t)(buf * TC_BN + h), v);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if constexpr (DF) {
+                    // error-free TwoSum of the exactly scaled block into (acc, lo)
 #pragma unroll
-                for (int q = 0; q < 32; ++q) acc[h + q] += v[q];
+                    for (int q = 0; q < 32; ++q) {
+                        const float x = v[q] * scl;
+                        const float sm = acc[h + q] + x;
+                        const float bp = sm - acc[h + q];
+                        lo[h + q] += (acc[h + q] - (sm - bp)) + (x - bp);
+                        acc[h + q] = sm;
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 32; ++q) acc[h + q] += v[q];
+                }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
@@ -291,8 +325,18 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
         if (failed) {
             if (lane == 0) *abort_flag = 1;
         } else if (nk > 0) {
-            epi((int64_t)blockIdx.z, row, n0, acc, M, N);
-            epi((int64_t)blockIdx.z, row, n0 + 32, acc + 32, M, N);
+            if constexpr (DF) {
+#pragma unroll
+                for (int h = 0; h < TC_BN; h += 32) {
+                    double d[32];
+#pragma unroll
+                    for (int q = 0; q < 32; ++q) d[q] = (double)acc[h + q] + (double)lo[h + q];
+                    epi((int64_t)blockIdx.z, row, n0 + h, d, M, N);
+                }
+            } else {
+                epi((int64_t)blockIdx.z, row, n0, acc, M, N);
+                epi((int64_t)blockIdx.z, row, n0 + 32, acc + 32, M, N);
+            }
         }
     }
     __syncthreads();
@@ -324,16 +368,21 @@ inline int tc_ksplit_count(int64_t nk, int want) {
 // ksplit) splits of the K range each produce a partial product (ks = 1 without split-K: z = b).
 // Both K maps must cover the same number of K blocks.  Every TMA x coordinate (koff + 32 j) is
 // a multiple of 4 floats (16 bytes).
-template <class EPI>
+template <class EPI, int FLUSH = 1, bool DF = false>
 int tc_gemm_tf32_mapped(cudaStream_t st, const TcOperand& A, const TcKMap& ka, const TcOperand& B, const TcKMap& kb,
                         int64_t batch, int64_t lower_div, const EPI& epi, int* err, int ksplit = 1) {
     if (A.rows <= 0 || B.rows <= 0 || batch <= 0) return 0;
+    if (FLUSH > 1 && (ksplit != 1 || ka.nkp % FLUSH || kb.nkp % FLUSH)) {
+        set_error(FORGE_ERR_ARG, "tc_gemm: exact-block mode needs whole flush groups per segment and no K split");
+        return FORGE_ERR_ARG;
+    }
     if ((A.ld % 4) || (B.ld % 4) || (A.batch_stride % 4) || (B.batch_stride % 4) || (ka.koff % 4) || (kb.koff % 4) ||
         ((uintptr_t)A.ptr % 16) || ((uintptr_t)B.ptr % 16)) {
         set_error(FORGE_ERR_ARG, "tc_gemm: operands must be 16-byte aligned with pitches multiple of 4 floats");
         return FORGE_ERR_ARG;
     }
-    if (ka.nkp * ka.nseg != kb.nkp * kb.nseg || ka.nseg < 1 || ka.nseg > 8 || kb.nseg < 1 || kb.nseg > 8) {
+    if (ka.nkp * ka.nseg != kb.nkp * kb.nseg || ka.nseg < 1 || ka.nseg > TC_MAXSEG || kb.nseg < 1 ||
+        kb.nseg > TC_MAXSEG) {
         set_error(FORGE_ERR_ARG, "tc_gemm: inconsistent K maps");
         return FORGE_ERR_ARG;
     }
@@ -342,7 +391,8 @@ int tc_gemm_tf32_mapped(cudaStream_t st, const TcOperand& A, const TcKMap& ka, c
     FORGE_TRY(tc_make_tmap(&mb, B, batch, TC_BN));
     static bool attr_set = false;
     if (!attr_set) {
-        FORGE_CUDA(cudaFuncSetAttribute(k_tc_gemm_tf32<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+        FORGE_CUDA(cudaFuncSetAttribute(k_tc_gemm_tf32<EPI, FLUSH, DF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        TC_SMEM));
         attr_set = true;
     }
     const int64_t nk = (int64_t)ka.nkp * ka.nseg;
@@ -354,8 +404,8 @@ int tc_gemm_tf32_mapped(cudaStream_t st, const TcOperand& A, const TcKMap& ka, c
     }
     dim3 grd((unsigned)((A.rows + TC_BM - 1) / TC_BM), (unsigned)((B.rows + TC_BN - 1) / TC_BN),
              (unsigned)(batch * ks));
-    k_tc_gemm_tf32<EPI><<<grd, TC_THREADS, TC_SMEM, st>>>(ma, mb, A.rows, B.rows, ka, kb, lower_div, ks, kchunk,
-                                                          epi, err);
+    k_tc_gemm_tf32<EPI, FLUSH, DF><<<grd, TC_THREADS, TC_SMEM, st>>>(ma, mb, A.rows, B.rows, ka, kb, lower_div, ks,
+                                                                     kchunk, epi, err);
     FORGE_LAUNCH_CHECK();
     return 0;
 }

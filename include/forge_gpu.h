@@ -88,6 +88,7 @@ typedef struct forge_iter_report {
     double residual;          /* max change of any H_HF element (eV) */
     int64_t nFermiLevel, nOccStates, nPartOccStates;
     int64_t info;             /* eigen-solver info of this iteration */
+    int64_t refined;          /* 1 if this iteration's eigenpairs were refined (forge_gpu_set_eigen_refinement) */
 } forge_iter_report;
 
 const char* forge_gpu_last_error(void);
@@ -210,6 +211,19 @@ int forge_gpu_set_mixing(forge_ctx* ctx, int64_t mode, int64_t depth, double bet
  * against the FP64 H(k): Y = H X, G = X^H Y, S = X^H X, then G z = theta S z on the host. */
 int forge_gpu_set_refinement(forge_ctx* ctx, int64_t width);
 
+/* Eigenpair refinement of the FORGE_PREC_MIXED eigen-solve (no counterpart in the reference, whose
+ * zheevr is FP64 throughout, LapackRoutines.f90:414-426): the mixed solve computes all ndim
+ * eigenpairs, then one Ogita-Aishima correction step makes eigenpairs 1..nUpper FP64-accurate.  The
+ * residual H X - X lam is an error-free product of integer slices on the tensor cores; the
+ * correction E = (X^H W) / (lam_j - lam_i) and X += X E use TF32 hi/lo products; pairs closer than
+ * delta (eV, default 1e-3) are only orthogonalised (FP64 overlaps).  The FP64 window Rayleigh-Ritz
+ * (forge_gpu_set_refinement) runs after it.  mode 0 = off (default), 1 = every mixed solve, 2 = the
+ * SCF solves from the first one after a residual below residual_below (eV) until the next guess or
+ * state load (forge_gpu_plain_guess, _field_guess, _set_state, _prepare_state).  depth 1..4 (0 = default 4):
+ * slice products s + t <= depth, relative accuracy of the residual ~2^-(25 + 9 depth). */
+int forge_gpu_set_eigen_refinement(forge_ctx* ctx, int64_t mode, double residual_below, double delta,
+                                   int64_t depth);
+
 /* nenforceC3 (Setup.f90:27): 1 selects Solve_C3 / GetFock_C3 (HartreeFock.f90:131-398, 564-881) in
  * every later solve and projector; 0 (the default) the full solve.  nC3pairs is the 1-based site map
  * of C3_RelatedPoints (Geometry.f90:1172-1223, a permutation), RotateLayers the nlayers layer
@@ -296,15 +310,17 @@ int forge_gpu_mlp_train(forge_mlp* mlp, const float* X, const float* targets, in
 
 /* Allocation-free eigen-solver (no counterpart in the reference): zdiagRed for one Hermitian
  * matrix (lower triangle of A, n x n complex, column-major) for callers that cannot allocate
- * device memory at call time (a memory pool or arena owning the whole GPU, latency-critical
- * loops where cudaMalloc would synchronise, hosts that manage every device buffer themselves).
- * A (overwritten), w (iu eigenvalues) and Z (n x iu complex eigenvectors) are DEVICE pointers;
- * stream is a cudaStream_t (NULL = default stream).  The workspace is a static device array of
- * FORGE_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library, so n is limited to
- * FORGE_NOALLOC_MAX_N; larger n is rejected with FORGE_ERR_ARG.  The first call on a device looks
- * up the array's device address: make it before any stream capture.  Calls share the array:
- * calls whose work overlaps on the GPU race.  Returns 0, 1 (inverse iteration did not converge)
- * or FORGE_ERR_*.  The solver is the FP64 path of forge_gpu_zheevr_batch. */
+ * device memory at call time (a memory pool or arena owning the whole GPU, hosts that manage
+ * every device buffer themselves).  A (overwritten), w (iu eigenvalues) and Z (n x iu complex
+ * eigenvectors) are DEVICE pointers; stream is a cudaStream_t (NULL = default stream).  The
+ * workspace is a static device array of FORGE_NOALLOC_SCRATCH_BYTES held by every GPU that loads
+ * the library, so 2 <= n <= FORGE_NOALLOC_MAX_N; other n are rejected with FORGE_ERR_ARG (n = 1
+ * needs no solver: w = Re A, Z = 1).  The first call on a device looks up the array's device
+ * address.  Every call ends by synchronising `stream` to read the solver's convergence flag, so
+ * the call blocks the host until its work is done and cannot be recorded into a CUDA graph.
+ * Calls share the array: calls whose work overlaps on the GPU race.  Returns 0, 1 (inverse
+ * iteration did not converge) or FORGE_ERR_*.  The solver is the FP64 path of
+ * forge_gpu_zheevr_batch. */
 #define FORGE_NOALLOC_MAX_N 512
 #define FORGE_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
 int forge_gpu_zheevr_noalloc(double* A, int64_t n, int64_t iu, double* w, double* Z, void* stream);

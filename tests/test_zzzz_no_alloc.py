@@ -1,11 +1,11 @@
 """Allocation-free eigen-solver entry point (forge_gpu_zheevr_noalloc).
 
 It exists for callers that cannot allocate device memory when they call the solver (a pool
-or arena owning the GPU, latency-critical loops, hosts that manage all device buffers); its
-workspace is a static device array.  Two calls in a row through the C-ABI must agree with the
-existing entry point forge_gpu_zheevr_batch within the FP64 tolerances the other tests use
-(eigenvalues 1e-12 relative, eigenvector projectors 1e-10).  This file is collected after the
-per-routine parity files.
+or arena owning the GPU, hosts that manage all device buffers); its workspace is a static
+device array.  Two calls in a row through the C-ABI must agree with the existing entry point
+forge_gpu_zheevr_batch within the FP64 tolerances the other tests use (eigenvalues 1e-12
+relative, eigenvector projectors 1e-10), and independently with LAPACK (numpy's eigh) to the
+same tolerances.  The file name sorts after every other test file, so pytest collects it last.
 """
 import ctypes as C
 
@@ -53,6 +53,11 @@ def test_noalloc_matches_batch_entry_point_twice(lib):
         Pn = Z[:, :k] @ Z[:, :k].conj().T
         Pb = Zb[:, :k, 0] @ Zb[:, :k, 0].conj().T
         assert np.max(np.abs(Pn - Pb)) <= 1e-10
+        # independent of the library's solver: LAPACK eigenvalues and occupied projector
+        wl, Zl = np.linalg.eigh(M)
+        assert np.max(np.abs(w - wl[:iu])) <= 1e-12 * np.max(np.abs(wl))
+        Pl = Zl[:, :k] @ Zl[:, :k].conj().T
+        assert np.max(np.abs(Pn - Pl)) <= 1e-10
         assert np.max(np.abs(Z.conj().T @ Z - np.eye(iu))) <= 1e-12
     for p in (dA, dw, dZ):
         rt.cudaFree(p)
