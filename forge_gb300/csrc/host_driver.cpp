@@ -12,6 +12,10 @@
 
 #include "forge_host.h"
 
+namespace forge {
+void set_error(int code, const char* fmt, ...);   // the library's error message (capi.cu)
+}
+
 namespace {
 
 const double kA1[2] = {0.5, 0.8660254037844386};   // [0.5, sqrt(3)*0.5]  Setup.f90:71
@@ -326,10 +330,28 @@ int forge_host_write_fock(const forge_setup* s, const double* zFock, const char*
 }
 
 int forge_host_read_fock(const forge_setup* s, double* zFock, const char* path, int64_t record_bytes) {
-    if (!s || !zFock || !path || record_bytes < 16) return FORGE_ERR_ARG;
+    if (!s || !zFock || !path || record_bytes < 16) {
+        forge::set_error(FORGE_ERR_ARG, "read_fock: null argument or record length below 16 bytes");
+        return FORGE_ERR_ARG;
+    }
     const int64_t N = s->ndim, NC = s->numNeighborCells;
     FILE* f = std::fopen(path, "rb");
-    if (!f) return FORGE_ERR_ARG;
+    if (!f) {
+        forge::set_error(FORGE_ERR_ARG, "read_fock: cannot open %s", path);
+        return FORGE_ERR_ARG;
+    }
+    // the whole record stream of Main.f90:647-672 and nothing else: a shorter file is a cut-off
+    // checkpoint, a longer one was written for another geometry or record length
+    const long long expect = ((long long)N * (N + 1) / 2 + (long long)(NC - 1) * N * N) * record_bytes;
+    std::fseek(f, 0, SEEK_END);
+    const long long have = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    if (have != expect) {
+        std::fclose(f);
+        forge::set_error(FORGE_ERR_ARG, "read_fock: %s holds %lld bytes, a checkpoint of ndim = %lld with %lld-byte "
+                         "records holds %lld", path, have, (long long)N, (long long)record_bytes, expect);
+        return FORGE_ERR_ARG;
+    }
     std::vector<unsigned char> row((size_t)N * record_bytes);
     const size_t NN = (size_t)N * N;
     bool ok = true;
@@ -355,7 +377,16 @@ int forge_host_read_fock(const forge_setup* s, double* zFock, const char* path, 
                 std::memcpy(zFock + 2 * (m * NN + (size_t)i + (size_t)j * N), row.data() + j * record_bytes, 16);
         }
     std::fclose(f);
-    return ok ? 0 : FORGE_ERR_ARG;
+    if (!ok) {
+        forge::set_error(FORGE_ERR_ARG, "read_fock: short read from %s", path);
+        return FORGE_ERR_ARG;
+    }
+    for (size_t q = 0; q < 2 * NN * (size_t)NC; ++q)
+        if (!std::isfinite(zFock[q])) {
+            forge::set_error(FORGE_ERR_NUMERIC, "read_fock: non-finite value in %s (element %zu)", path, q / 2);
+            return FORGE_ERR_NUMERIC;
+        }
+    return 0;
 }
 
 // SortEnergies_2Spins (HartreeFock.f90:929-1004).  Counters are 1-based as in the reference; the

@@ -246,12 +246,18 @@ def apply(hf: HartreeFock, setup: Setup, ws: Optional[WarmStart] = None, path: s
             raise ForgeError(-1, f"warm-start weights not found at {path}")
         ws = WarmStart.load(path)
     P = predicted_state(hf, ws)
+    if not np.all(np.isfinite(P)):
+        # a network that produced NaN / Inf (corrupt weights, out-of-range descriptors) is not used
+        hf.warm_start_residuals = (float("nan"), float("nan"))
+        E2, _ = hf.PlainGuess()
+        hf.warm_start_used = False
+        return tuple(E2)
     E = np.zeros(4)
     res = np.zeros(2)
     rc = hf.lib.forge_gpu_field_guess(hf.ctx, _ptr(np.asfortranarray(P)), _ptr(E), _ptr(res))
     _check(rc, allow_info=True)
     hf.warm_start_residuals = (float(res[0]), float(res[1]))
-    if res[0] >= res[1]:
+    if not (res[0] < res[1]):          # also when a residual is NaN
         E2, _ = hf.PlainGuess()
         hf.warm_start_used = False
         return tuple(E2)

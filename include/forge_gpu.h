@@ -4,7 +4,7 @@
  * Drop-in boundary for the hot path of FORGE (forge-team/forge, Fortran 90):
  * every entry point replaces one routine of HartreeFock.f90 / LapackRoutines.f90
  * or one inline loop of Main.f90, with the same argument meaning.  A Fortran
- * host binds these with ISO_C_BINDING (interface blocks in INTEGRATION.md).
+ * host binds these with ISO_C_BINDING.
  *
  * Conventions
  *   - integers are int64_t (the reference's integer(dp)), reals are double (real(dp));
@@ -278,18 +278,6 @@ int forge_gpu_timer_mark(forge_ctx* ctx, int64_t slot);
 int forge_gpu_timer_elapsed(forge_ctx* ctx, int64_t slot_a, int64_t slot_b, double* ms);
 int forge_gpu_profile_read(forge_ctx* ctx, double* ms, int64_t* launches, double* bytes, double* flops,
                            int64_t n);
-
-/* Diagnostic (no counterpart in the reference): D = A B^T on the tcgen05 tensor cores with
- * TF32 inputs and FP32 accumulation; A (batch x M x K), B (batch x N x K), D (batch x M x N),
- * all row-major fp32 host arrays.  Used by the tests to validate the tensor-core GEMM. */
-int forge_gpu_selftest_tc_gemm(int64_t M, int64_t N, int64_t K, int64_t batch, const float* A, const float* B,
-                               float* D);
-
-/* Diagnostic, host only: the small dense step of the window refinement.  G, S: n x n Hermitian
- * (complex, column-major, interleaved re/im doubles), n <= 32.  Returns theta (ascending) and
- * M = L^{-H} U, with S = L L^H and L^{-1} G L^{-H} = U diag(theta) U^H, so that G M = S M diag(theta)
- * and M^H S M = I.  Returns 1 if S is not positive definite. */
-int forge_selftest_rr_small(int64_t n, const double* G, const double* S, double* theta, double* M);
 
 /* Learned SCF warm start (no counterpart in the reference, which starts from the non-interacting
  * guess or a checkpoint): an MLP din -> 128 -> 128 -> 128 -> dout (SiLU), BF16 weights, FP32

@@ -46,13 +46,23 @@ def test_tc_gemm_tf32_error_bound(lib):
     assert np.all(np.abs(D[0] - ref) <= bound)
 
 
+def _tf32(x):
+    """Rounds toward zero to the 10-bit TF32 mantissa (the values are then exact in TF32)."""
+    b = np.asarray(x, np.float32).view(np.uint32) & np.uint32(0xFFFFE000)
+    return b.view(np.float32)
+
+
 def test_tc_gemm_accumulation_bias_is_bounded(lib):
     """With TF32-exact all-positive operands the tensor core's FP32 accumulation truncates (measured
     -5.9e-5 relative at K = 8192 with one TMEM accumulator); the kernel accumulates each K block of 32
     alone and sums the blocks in round-to-nearest FP32 registers, which bounds the bias near -9e-8
-    independently of K (forge_gb300.tcbias)."""
-    from forge_gb300 import tcbias
+    independently of K."""
+    rng = np.random.default_rng(0)
+    M = N = 256
     for K in (512, 8192):
-        r = tcbias.measure(K, positive=True)
-        assert r["rc"] == 0
-        assert abs(r["mean_rel"]) <= 3e-7, r
+        A = _tf32(rng.uniform(0.5, 1.0, (1, M, K)))
+        B = _tf32(rng.uniform(0.5, 1.0, (1, N, K)))
+        D = _tc(lib, A, B)
+        ref = A[0].astype(np.float64) @ B[0].astype(np.float64).T
+        rel = (D[0] - ref) / np.abs(ref).max()
+        assert abs(float(rel.mean())) <= 3e-7, (K, float(rel.mean()))

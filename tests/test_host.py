@@ -14,7 +14,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def _declared_symbols():
     names = set()
-    for h in ("forge_gpu.h", "forge_host.h"):
+    for h in ("forge_gpu.h", "forge_host.h", "forge_gpu_selftest.h"):
         txt = open(os.path.join(ROOT, "include", h)).read()
         names |= set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(forge_\w+)\s*\(", txt, flags=re.M))
     return names
@@ -132,6 +132,33 @@ def test_fock_checkpoint_rejects_missing_file(tmp_path):
     import forge_gb300 as fg
     with pytest.raises(fg.ForgeError):
         fg.read_fock(fg.Setup(ntheta=2, numk=1), str(tmp_path / "missing"), 16)
+
+
+@pytest.mark.parametrize("damage", ["truncated", "trailing", "nan", "other_record_length"])
+def test_fock_checkpoint_rejects_damaged_file(tmp_path, damage):
+    """A restart (Main.f90:202-234) must not load a cut-off, padded or corrupted checkpoint, nor one
+    written with another record length: the reader fails with a message instead."""
+    import forge_gb300 as fg
+    S = fg.Setup(ntheta=2, numk=1)
+    N = S.to_struct().ndim
+    rng = np.random.default_rng(3)
+    P = np.asfortranarray(rng.standard_normal((N, N, 4)) + 1j * rng.standard_normal((N, N, 4)))
+    path = str(tmp_path / "Fock")
+    fg.write_fock(S, P, path, 16)
+    data = bytearray(open(path, "rb").read())
+    rb = 16
+    if damage == "truncated":
+        data = data[: len(data) // 2]
+    elif damage == "trailing":
+        data += b"\0" * 16
+    elif damage == "nan":
+        data[16 * 5: 16 * 5 + 8] = np.float64(np.nan).tobytes()
+    else:
+        rb = 64
+    open(path, "wb").write(bytes(data))
+    with pytest.raises(fg.ForgeError) as e:
+        fg.read_fock(S, path, rb)
+    assert ("non-finite" if damage == "nan" else "bytes") in str(e.value)
 
 
 @pytest.mark.parametrize("n,seed", [(1, 0), (5, 1), (32, 2)])
