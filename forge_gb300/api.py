@@ -91,6 +91,8 @@ SIGNATURES = {
     "forge_gpu_prepare_state": [_P, _P],
     "forge_gpu_field_guess": [_P, _P, _P, _P],
     "forge_gpu_scf_iteration": [_P, _P, _P],
+    "forge_gpu_solve_group": [_P, _I, _P],
+    "forge_gpu_scf_iteration_group": [_P, _I, _P, _P],
     "forge_gpu_set_precision": [_P, _I],
     "forge_gpu_set_mixing": [_P, _I, _I, C.c_double],
     "forge_gpu_set_refinement": [_P, _I],
@@ -568,3 +570,28 @@ class HartreeFock:
         self.lib.forge_gpu_profile_read(self.ctx, _ptr(ms), _ptr(nl), _ptr(b), _ptr(f), n)
         return {s: dict(ms=float(ms[i]), launches=int(nl[i]), bytes=float(b[i]), flops=float(f[i]))
                 for i, s in enumerate(self.STAGES)}
+
+
+def _ctx_array(contexts: Sequence["HartreeFock"]):
+    arr = (C.c_void_p * len(contexts))(*[h.ctx.value if isinstance(h.ctx, C.c_void_p) else h.ctx for h in contexts])
+    return arr
+
+
+def SolveGroup(contexts: Sequence["HartreeFock"]):
+    """One batched eigen-solve over every H(k) of several systems of different ndim
+    (forge_gpu_solve_group); returns the per-context info counts."""
+    lib = load_library()
+    info = np.zeros(len(contexts), np.int64)
+    _check(lib.forge_gpu_solve_group(_ctx_array(contexts), len(contexts), _ptr(info)), allow_info=True)
+    return info
+
+
+def ScfIterationGroup(contexts: Sequence["HartreeFock"], energies):
+    """One SCF iteration of each context with a shared uneven-size batched eigen-solve
+    (forge_gpu_scf_iteration_group): returns (reports, energies (n x 4), info)."""
+    lib = load_library()
+    E = np.ascontiguousarray(energies, dtype=np.float64).reshape(len(contexts), 4).copy()
+    reps = (forge_iter_report * len(contexts))()
+    info = _check(lib.forge_gpu_scf_iteration_group(_ctx_array(contexts), len(contexts), _ptr(E), reps),
+                  allow_info=True)
+    return [reps[i].as_dict() for i in range(len(contexts))], E, info

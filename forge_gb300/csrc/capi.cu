@@ -80,6 +80,8 @@ int rr_window(cudaStream_t st, const double2* H, int64_t strideH, double2* X, in
 size_t rr_window_workspace_bytes(int64_t n, int64_t batch);
 const float* eig_mixed_planes(void* mixed_ws, int64_t n, int64_t iu, int64_t batch, int64_t* n4);
 size_t oa_workspace_bytes(int64_t n, int64_t iu);
+int launch_pad_slot(cudaStream_t st, const double2* src, int64_t nb, double2* dst, int64_t n, double* rowsum,
+                    double* sigma);
 int oa_refine(cudaStream_t st, double2* H, int64_t strideH, const float* Xs, int64_t n4, int64_t nall,
               const double* lam, int64_t n, int64_t iu, int64_t batch, double2* X, int64_t ldx, int64_t strideX,
               double* w_out, int64_t w_stride, void* ws, int* err, double delta, int depth);
@@ -108,6 +110,8 @@ struct forge_ctx {
     bool oa_active = false, oa_latched = false;
     double last_residual = INFINITY;
     DevBuf oaws, w_all;
+    // group solve led by this context (forge_gpu_solve_group): padded H slots, eigenpairs, workspaces
+    DevBuf g_H, g_X, g_w, g_eigws, g_mixws, g_tmp, g_rows, g_sig, g_rr;
     int64_t eig_batch = 0;
     int64_t k_begin = 0, k_end = 0;  // local k range (k_end = 0: all k)
     // mixing: FORGE_MIX_ODA (OptimalStep, the reference) or FORGE_MIX_PULAY (Anderson / Pulay)
@@ -803,6 +807,185 @@ int pulay_mix(forge_ctx* x) {
     return scf_diis_commit(c, sc);
 }
 
+// One batched eigen-solve over the H(k) of every k of several contexts of different ndim (the
+// uneven-size batch): each H(k) is assembled by its own context into a scratch matrix, embedded in
+// an nmax x nmax slot (launch_pad_slot), the slots are solved in batches by the context precision's
+// solver (zdiagRed, iu = the largest nUpper), the mixed path's FP64 window Rayleigh-Ritz runs per
+// slot on that system's own window, and each context receives its eigenpairs 1..nUpper.  All
+// work runs on the first context's stream.
+int solve_group_device(forge_ctx** xs, int64_t nctx, int* infos) {
+    forge_ctx* x0 = xs[0];
+    Context& c0 = x0->c;
+    cudaStream_t st = c0.stream;
+    int64_t nmax = 0, iumax = 0;
+    std::vector<std::pair<int64_t, int64_t>> items;
+    for (int64_t b = 0; b < nctx; ++b) {
+        forge_ctx* x = xs[b];
+        Context& c = x->c;
+        if (c.precision != c0.precision || x->c3 || x->valley || x->k_begin != 0 || x->k_end != 0 || x->oa_mode != 0) {
+            set_error(FORGE_ERR_ARG, "solve_group: context %lld differs in precision or uses C3, valley, k shards or "
+                      "the eigenpair refinement (not available in a group)", (long long)b);
+            return FORGE_ERR_ARG;
+        }
+        if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
+        nmax = std::max<int64_t>(nmax, c.N);
+        iumax = std::max<int64_t>(iumax, c.nUpper);
+        for (int64_t k = 0; k < c.Nk; ++k) items.push_back({b, k});
+        FORGE_TRY(c.X.ensure((size_t)c.Nk * c.N * c.nUpper * sizeof(double2)));
+        FORGE_TRY(x->w.ensure((size_t)c.Nk * c.nUpper * sizeof(double)));
+        FORGE_TRY(c.bulk.ensure(4 * (size_t)c.N * c.N * sizeof(double2)));
+        infos[b] = 0;
+    }
+    const bool mixed = c0.precision == FORGE_PREC_MIXED;
+    const size_t slot = (size_t)nmax * nmax;
+    size_t per_item = slot * 16 + eig_workspace_bytes(nmax, iumax, 1) + (size_t)nmax * iumax * 16 + iumax * 8;
+    if (mixed) per_item += eig_mixed_workspace_bytes(nmax, iumax, 1);
+    size_t freeb = 0, totalb = 0;
+    cudaMemGetInfo(&freeb, &totalb);
+    const size_t reserve = ((size_t)8 << 30) + slot * 16;
+    int64_t B = (int64_t)((freeb > reserve ? freeb - reserve : freeb / 4) / per_item);
+    B = std::max<int64_t>(1, std::min<int64_t>(B, (int64_t)items.size()));
+    FORGE_TRY(x0->g_H.ensure((size_t)B * slot * sizeof(double2)));
+    FORGE_TRY(x0->g_X.ensure((size_t)B * nmax * iumax * sizeof(double2)));
+    FORGE_TRY(x0->g_w.ensure((size_t)B * iumax * sizeof(double)));
+    FORGE_TRY(x0->g_eigws.ensure(eig_workspace_bytes(nmax, iumax, B)));
+    if (mixed) FORGE_TRY(x0->g_mixws.ensure(eig_mixed_workspace_bytes(nmax, iumax, B)));
+    FORGE_TRY(x0->g_tmp.ensure(slot * sizeof(double2)));
+    FORGE_TRY(x0->g_rows.ensure(nmax * sizeof(double)));
+    FORGE_TRY(x0->g_sig.ensure(sizeof(double)));
+    if (mixed && x0->rr_width > 0) FORGE_TRY(x0->g_rr.ensure(rr_window_workspace_bytes(nmax, 1)));
+    double2* gH = x0->g_H.as<double2>();
+    double2* gX = x0->g_X.as<double2>();
+    double* gw = x0->g_w.as<double>();
+    for (size_t q0 = 0; q0 < items.size(); q0 += (size_t)B) {
+        const int64_t nb = std::min<int64_t>(B, (int64_t)(items.size() - q0));
+        for (int64_t q = 0; q < nb; ++q) {
+            Context& cb = xs[items[q0 + q].first]->c;
+            const cudaStream_t own = cb.stream;
+            cb.stream = st;   // the assembly of every member on the group's stream
+            const int rc = launch_assemble(cb, cb.V.as<double>(), cb.P.as<double2>(), items[q0 + q].second, 1,
+                                           x0->g_tmp.as<double2>());
+            cb.stream = own;
+            FORGE_TRY(rc);
+            FORGE_TRY(launch_pad_slot(st, x0->g_tmp.as<double2>(), cb.N, gH + q * slot, nmax, x0->g_rows.as<double>(),
+                                      x0->g_sig.as<double>()));
+        }
+        EigArgs g{};
+        g.n = nmax;
+        g.iu = iumax;
+        g.batch = nb;
+        g.A = gH;
+        g.lda = nmax;
+        g.strideA = (int64_t)slot;
+        g.X = gX;
+        g.ldx = nmax;
+        g.strideX = nmax * iumax;
+        g.w = gw;
+        g.ortol_rel = 1e-7;
+        eig_bind_workspace(g, x0->g_eigws.ptr);
+        FORGE_TRY(mixed ? eig_mixed(st, g, x0->g_mixws.ptr) : eig_fp64(st, g));
+        if (mixed && x0->rr_width > 0)
+            for (int64_t q = 0; q < nb; ++q) {
+                const int64_t iub = xs[items[q0 + q].first]->c.nUpper;
+                const int64_t nw = std::min<int64_t>(x0->rr_width, iub);
+                FORGE_TRY(rr_window(st, gH + q * slot, (int64_t)slot, gX + q * nmax * iumax, nmax, nmax * iumax,
+                                    gw + q * iumax, iumax, nmax, iub - nw, nw, 1, x0->g_rr.ptr));
+            }
+        std::vector<int> fails(nb);
+        FORGE_CUDA(cudaMemcpyAsync(fails.data(), g.fail, nb * sizeof(int), cudaMemcpyDeviceToHost, st));
+        for (int64_t q = 0; q < nb; ++q) {
+            const int64_t b = items[q0 + q].first, k = items[q0 + q].second;
+            Context& cb = xs[b]->c;
+            const int64_t Nb = cb.N, iub = cb.nUpper;
+            FORGE_CUDA(cudaMemcpy2DAsync(cb.X.as<double2>() + (size_t)k * Nb * iub, Nb * sizeof(double2),
+                                         gX + q * nmax * iumax, nmax * sizeof(double2), Nb * sizeof(double2), iub,
+                                         cudaMemcpyDeviceToDevice, st));
+            FORGE_CUDA(cudaMemcpyAsync(xs[b]->w.as<double>() + (size_t)k * iub, gw + q * iumax, iub * sizeof(double),
+                                       cudaMemcpyDeviceToDevice, st));
+        }
+        FORGE_CUDA(cudaStreamSynchronize(st));
+        for (int64_t q = 0; q < nb; ++q) infos[items[q0 + q].first] += fails[q] ? 1 : 0;
+    }
+    for (int64_t b = 0; b < nctx; ++b) {
+        forge_ctx* x = xs[b];
+        Context& c = x->c;
+        x->h_bph.resize(c.Nk * 4);
+        FORGE_CUDA(cudaMemcpy(x->h_bph.data(), c.bphase.ptr, c.Nk * 4 * sizeof(double2), cudaMemcpyDeviceToHost));
+        x->oa_active = false;
+        x->have_solve = true;
+        x->have_sort = false;
+        x->bulk_is_fused = true;
+    }
+    return 0;
+}
+
+// forge_gpu_scf_iteration before its solve: checks, the input energies into the device scalars
+int scf_iteration_begin(forge_ctx* x, double* Energies, double* Ein) {
+    Context& c = x->c;
+    if (!x->have_state) {
+        set_error(FORGE_ERR_STATE, "scf_iteration needs plain_guess or set_state + prepare_state first");
+        return FORGE_ERR_STATE;
+    }
+    if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
+    ScfScalars h;
+    FORGE_TRY(read_scalars(x, &h));
+    if (Energies) {
+        for (int t = 0; t < 4; ++t) h.Ein[t] = Energies[t];
+        FORGE_TRY(write_scalars(x, &h));
+    }
+    for (int t = 0; t < 4; ++t) Ein[t] = h.Ein[t];
+    return 0;
+}
+
+// forge_gpu_scf_iteration after its solve (eigenpairs of every k in c.X / w): sort, Fermi level,
+// P_new, energies, mixing and potential (Main.f90:392-595), and the report
+int scf_iteration_end(forge_ctx* x, const double* Ein, int info, double* Energies, forge_iter_report* rep) {
+    Context& c = x->c;
+    FORGE_TRY(sort_device(x, c.s.nfilling));
+    FORGE_TRY(x->valley ? project_valley(x) : project_fused(x));
+    FORGE_TRY(symmetrize_pnew(x));
+    FORGE_TRY(scf_density(c, x->Pn.as<double2>(), x->dens_new.as<double>()));
+    FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(),
+                               x->dens_new.as<double>(), x->y.as<double>(), x->work.as<double>(),
+                               x->sc.as<ScfScalars>()));
+    if (x->mix_mode == FORGE_MIX_PULAY) {
+        FORGE_TRY(pulay_mix(x));
+    } else {
+        FORGE_TRY(scf_oda(c, x->sc.as<ScfScalars>(), 0));
+        FORGE_TRY(scf_mix(c, c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(), c.V.as<double>(),
+                          x->y.as<double>(), x->work.as<double>(), x->sc.as<ScfScalars>()));
+    }
+    ScfScalars h;
+    FORGE_TRY(read_scalars(x, &h));
+    x->have_pnew = false;
+    x->last_residual = h.residual;
+    if (Energies)
+        for (int t = 0; t < 4; ++t) Energies[t] = h.Eout[t];
+    if (rep) {
+        rep->refined = x->oa_active ? 1 : 0;
+        rep->Step = h.step;
+        rep->DensityConvergence = h.dn_max;
+        rep->TotalEnergyIn = h.Etot_in;
+        rep->TotalEnergy = h.Etot_out;
+        rep->KineticEnergyIn = Ein[0];
+        rep->FockEnergyIn = Ein[1];
+        rep->HartreeEnergyIn = Ein[2];
+        rep->HubbardEnergyIn = Ein[3];
+        rep->KineticEnergy = h.Eout[0];
+        rep->FockEnergy = h.Eout[1];
+        rep->HartreeEnergy = h.Eout[2];
+        rep->HubbardEnergy = h.Eout[3];
+        rep->FermiEnergy = h.EF;
+        rep->DegFactor = h.DegFactor;
+        rep->residual = h.residual;
+        rep->nFermiLevel = h.nF;
+        rep->nOccStates = h.nOcc;
+        rep->nPartOccStates = h.nPart;
+        rep->info = info;
+    }
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -944,7 +1127,8 @@ int forge_gpu_finalize(forge_ctx* x) {
                       &x->projws, &x->tcerr, &x->diis_hist, &x->diis_rprev, &x->diis_part, &x->rrws, &x->pstates,
                       &x->c3_Xr, &x->c3_wr, &x->c3_tab, &x->c3_perm, &x->c3_phase, &x->c2_perm,
                       &x->v_rowp, &x->v_col, &x->v_coef, &x->v_code, &x->v_ph, &x->v_W, &x->v_G, &x->v_S,
-                      &x->v_Xv, &x->v_st, &x->oaws, &x->w_all};
+                      &x->v_Xv, &x->v_st, &x->oaws, &x->w_all, &x->g_H, &x->g_X, &x->g_w, &x->g_eigws,
+                      &x->g_mixws, &x->g_tmp, &x->g_rows, &x->g_sig, &x->g_rr};
     for (DevBuf* b : bufs) b->release();
     if (c.stream) cudaStreamDestroy(c.stream);
     delete x;
@@ -1778,65 +1962,53 @@ int forge_gpu_prepare_state(forge_ctx* x, double* Energies) {
     return prepare_state_device(x, Energies);
 }
 
+int forge_gpu_solve_group(forge_ctx** ctxs, int64_t nctx, int64_t* info) {
+    if (!ctxs || nctx < 1) {
+        set_error(FORGE_ERR_ARG, "solve_group: no contexts");
+        return FORGE_ERR_ARG;
+    }
+    for (int64_t b = 0; b < nctx; ++b) FORGE_TRY(check_ctx(ctxs[b]));
+    FORGE_TRY(check_ctx(ctxs[0]));
+    std::vector<int> infos(nctx, 0);
+    FORGE_TRY(solve_group_device(ctxs, nctx, infos.data()));
+    int bad = 0;
+    for (int64_t b = 0; b < nctx; ++b) {
+        if (info) info[b] = infos[b];
+        bad += infos[b];
+    }
+    return bad;
+}
+
+int forge_gpu_scf_iteration_group(forge_ctx** ctxs, int64_t nctx, double* Energies, forge_iter_report* reports) {
+    if (!ctxs || nctx < 1) {
+        set_error(FORGE_ERR_ARG, "scf_iteration_group: no contexts");
+        return FORGE_ERR_ARG;
+    }
+    std::vector<double> Ein(4 * nctx);
+    for (int64_t b = 0; b < nctx; ++b) {
+        FORGE_TRY(check_ctx(ctxs[b]));
+        FORGE_TRY(scf_iteration_begin(ctxs[b], Energies ? Energies + 4 * b : nullptr, &Ein[4 * b]));
+    }
+    FORGE_TRY(check_ctx(ctxs[0]));
+    std::vector<int> infos(nctx, 0);
+    FORGE_TRY(solve_group_device(ctxs, nctx, infos.data()));
+    int bad = 0;
+    for (int64_t b = 0; b < nctx; ++b) {
+        FORGE_TRY(check_ctx(ctxs[b]));
+        FORGE_TRY(scf_iteration_end(ctxs[b], &Ein[4 * b], infos[b], Energies ? Energies + 4 * b : nullptr,
+                                    reports ? reports + b : nullptr));
+        bad += infos[b];
+    }
+    return bad;
+}
+
 int forge_gpu_scf_iteration(forge_ctx* x, double* Energies, forge_iter_report* rep) {
     FORGE_TRY(check_ctx(x));
-    Context& c = x->c;
-    if (!x->have_state) {
-        set_error(FORGE_ERR_STATE, "scf_iteration needs plain_guess or set_state + prepare_state first");
-        return FORGE_ERR_STATE;
-    }
-    if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
-    ScfScalars h;
-    FORGE_TRY(read_scalars(x, &h));
-    if (Energies) {
-        for (int t = 0; t < 4; ++t) h.Ein[t] = Energies[t];
-        FORGE_TRY(write_scalars(x, &h));
-    }
     double Ein[4];
-    for (int t = 0; t < 4; ++t) Ein[t] = h.Ein[t];
+    FORGE_TRY(scf_iteration_begin(x, Energies, Ein));
     int info = 0;
     FORGE_TRY(solve_device(x, &info, false));
-    FORGE_TRY(sort_device(x, c.s.nfilling));
-    FORGE_TRY(x->valley ? project_valley(x) : project_fused(x));
-    FORGE_TRY(symmetrize_pnew(x));
-    FORGE_TRY(scf_density(c, x->Pn.as<double2>(), x->dens_new.as<double>()));
-    FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(),
-                               x->dens_new.as<double>(), x->y.as<double>(), x->work.as<double>(),
-                               x->sc.as<ScfScalars>()));
-    if (x->mix_mode == FORGE_MIX_PULAY) {
-        FORGE_TRY(pulay_mix(x));
-    } else {
-        FORGE_TRY(scf_oda(c, x->sc.as<ScfScalars>(), 0));
-        FORGE_TRY(scf_mix(c, c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(), c.V.as<double>(),
-                          x->y.as<double>(), x->work.as<double>(), x->sc.as<ScfScalars>()));
-    }
-    FORGE_TRY(read_scalars(x, &h));
-    x->have_pnew = false;
-    x->last_residual = h.residual;
-    if (Energies)
-        for (int t = 0; t < 4; ++t) Energies[t] = h.Eout[t];
-    if (rep) {
-        rep->refined = x->oa_active ? 1 : 0;
-        rep->Step = h.step;
-        rep->DensityConvergence = h.dn_max;
-        rep->TotalEnergyIn = h.Etot_in;
-        rep->TotalEnergy = h.Etot_out;
-        rep->KineticEnergyIn = Ein[0];
-        rep->FockEnergyIn = Ein[1];
-        rep->HartreeEnergyIn = Ein[2];
-        rep->HubbardEnergyIn = Ein[3];
-        rep->KineticEnergy = h.Eout[0];
-        rep->FockEnergy = h.Eout[1];
-        rep->HartreeEnergy = h.Eout[2];
-        rep->HubbardEnergy = h.Eout[3];
-        rep->FermiEnergy = h.EF;
-        rep->DegFactor = h.DegFactor;
-        rep->residual = h.residual;
-        rep->nFermiLevel = h.nF;
-        rep->nOccStates = h.nOcc;
-        rep->nPartOccStates = h.nPart;
-        rep->info = info;
-    }
+    FORGE_TRY(scf_iteration_end(x, Ein, info, Energies, rep));
     return info;
 }
 

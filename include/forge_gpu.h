@@ -195,6 +195,19 @@ int forge_gpu_prepare_state(forge_ctx* ctx, double* Energies);
  * Energies[4] as in optimal_step (in: current, out: new). */
 int forge_gpu_scf_iteration(forge_ctx* ctx, double* Energies, forge_iter_report* report);
 
+/* Uneven-size batch (no counterpart in the reference, which builds one system per binary,
+ * Setup.f90:6-74): the Solve eigen-step of nctx contexts of different ndim (same precision, same
+ * device, no C3 / valley / k shard / eigenpair refinement) as ONE batched eigen-solve.  Every H(k)
+ * of every context is embedded in an nmax x nmax slot (nmax = the largest ndim) with a Gershgorin
+ * shift s > every eigenvalue on the padded diagonal, which decouples exactly, so each context gets
+ * the eigenpairs 1..nUpper of its own H(k) (plus the FP64 window Rayleigh-Ritz of its own window in
+ * mixed precision).  info[b] (NULL allowed): number of k of context b whose solve did not converge.
+ * The work runs on ctxs[0]'s stream and its group buffers. */
+int forge_gpu_solve_group(forge_ctx** ctxs, int64_t nctx, int64_t* info);
+/* One SCF iteration of each context (forge_gpu_scf_iteration) with the eigen-solve shared as in
+ * forge_gpu_solve_group: Energies is nctx x 4 (NULL allowed), reports nctx (NULL allowed). */
+int forge_gpu_scf_iteration_group(forge_ctx** ctxs, int64_t nctx, double* Energies, forge_iter_report* reports);
+
 /* Mixing of forge_gpu_scf_iteration (no counterpart in the reference, which mixes with OptimalStep
  * only):
  * FORGE_MIX_ODA (default) or FORGE_MIX_PULAY with `depth` (1..7) previous steps and mixing weight
