@@ -105,6 +105,7 @@ SIGNATURES = {
     "forge_gpu_timer_elapsed": [_P, _I, _I, _P],
     "forge_gpu_profile_read": [_P, _P, _P, _P, _P, _I],
     "forge_gpu_selftest_tc_gemm": [_I, _I, _I, _I, _P, _P, _P],
+    "forge_gpu_selftest_tc_gemm_timeout": [_I, _I, _I, _I, _P, _P, _P],
     "forge_gpu_mlp_create": [_I, _I, C.c_uint64, _P],
     "forge_gpu_mlp_destroy": [_P],
     "forge_gpu_mlp_set_params": [_P, _P],

@@ -166,8 +166,11 @@ int choose_batch(forge_ctx* x) {
     // kept free: 8 GB headroom, the eigenvectors of every k, the four bulk cells and the
     // projector / window work arrays allocated after the batch is chosen
     const int64_t xslots = x->c3 ? x->c3t.nslots + (int64_t)x->c3t.reps.size() : c.Nk;
+    // the Pulay history (depth + 1 slots of dX, dR and the previous residual, complex64 over the four
+    // cells) is allocated at the first mixing step, after this choice
+    const size_t diis = x->mix_mode == FORGE_MIX_PULAY ? ((size_t)(2 * (x->diis_depth + 1) + 1) * 4 * N * N * 8) : 0;
     const size_t reserve = ((size_t)8 << 30) + (size_t)xslots * N * iu * 16 + (size_t)10 * N * N * 16 +
-                           (oa ? oa_workspace_bytes(N, iu) : 0);
+                           (oa ? oa_workspace_bytes(N, iu) : 0) + diis;
     const size_t budget = freeb > reserve ? freeb - reserve : freeb / 4;
     int64_t b = (int64_t)(budget / per_k);
     // FORGE_EIG_BATCH caps the number of k points solved per launch (memory control)

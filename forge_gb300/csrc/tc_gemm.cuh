@@ -84,10 +84,19 @@ __device__ inline void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
 __device__ inline void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
+// Failure-injection controls of one launch (test hooks): the iteration bound of every mbarrier
+// wait, and a K block at which the TMA producer stops issuing (-1: never), so that the MMA issuer's
+// wait for that block runs out.  Normal launches use {TC_SPIN_LIMIT, -1}.
+struct TcFault {
+    uint32_t spin_limit = TC_SPIN_LIMIT;
+    int32_t stop_loads_at = -1;
+};
+
 // returns false if the wait gave up
-__device__ inline bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+__device__ inline bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                 uint32_t limit = TC_SPIN_LIMIT) {
     uint32_t done = 0;
-    for (uint32_t it = 0; it < TC_SPIN_LIMIT; ++it) {
+    for (uint32_t it = 0; it < limit; ++it) {
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(done)
@@ -140,9 +149,10 @@ __device__ inline void tc_commit(uint64_t* bar) {
 }
 
 // one lane polls, the warp gets the result (tcgen05.ld needs the whole warp on the same path)
-__device__ inline bool mbar_wait_warp(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+__device__ inline bool mbar_wait_warp(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                      uint32_t limit = TC_SPIN_LIMIT) {
     int ok = 0;
-    if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, abort_flag) ? 1 : 0;
+    if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, abort_flag, limit) ? 1 : 0;
     return __shfl_sync(0xffffffffu, ok, 0) != 0;
 }
 
@@ -164,7 +174,7 @@ template <class EPI, int FLUSH = 1, bool DF = false>
 __global__ void __launch_bounds__(TC_THREADS, DF ? 1 : 2)
     k_tc_gemm_tf32(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int64_t M,
                    int64_t N, const __grid_constant__ TcKMap ka, const __grid_constant__ TcKMap kb_map,
-                   int64_t lower_div, int32_t ksplit, int32_t kchunk, EPI epi, int* err) {
+                   int64_t lower_div, int32_t ksplit, int32_t kchunk, EPI epi, int* err, TcFault flt) {
     // lower_div > 0: skip tiles whose rows (divided by lower_div) all lie above the diagonal
     if (lower_div > 0 && ((int64_t)blockIdx.x * TC_BM + TC_BM - 1) / lower_div < (int64_t)blockIdx.y * TC_BN) return;
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
@@ -221,7 +231,8 @@ __global__ void __launch_bounds__(TC_THREADS, DF ? 1 : 2)
             for (int kb = 0; kb < nk; ++kb) {
                 const int s = kb % TC_STAGES;
                 const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
-                if (kb >= TC_STAGES && !mbar_wait(&empty[s], ph ^ 1u, abort_flag)) {
+                if (kb == flt.stop_loads_at) break;   // failure injection: this block never arrives
+                if (kb >= TC_STAGES && !mbar_wait(&empty[s], ph ^ 1u, abort_flag, flt.spin_limit)) {
                     *abort_flag = 1;
                     break;
                 }
@@ -248,11 +259,12 @@ __global__ void __launch_bounds__(TC_THREADS, DF ? 1 : 2)
                 const int grp = kb / FLUSH, buf = grp & 1, use = grp >> 1;
                 const bool first = (kb % FLUSH) == 0;
                 const bool last = (kb % FLUSH) == FLUSH - 1 || kb == nk - 1;
-                if (!mbar_wait(&full[s], ph, abort_flag)) {
+                if (!mbar_wait(&full[s], ph, abort_flag, flt.spin_limit)) {
                     *abort_flag = 1;
                     break;
                 }
-                if (first && use > 0 && !mbar_wait(&tfree[buf], (uint32_t)(use - 1) & 1u, abort_flag)) {
+                if (first && use > 0 &&
+                    !mbar_wait(&tfree[buf], (uint32_t)(use - 1) & 1u, abort_flag, flt.spin_limit)) {
                     *abort_flag = 1;
                     break;
                 }
@@ -288,7 +300,7 @@ __global__ void __launch_bounds__(TC_THREADS, DF ? 1 : 2)
         const int ngrp = (nk + FLUSH - 1) / FLUSH;
         for (int grp = 0; grp < ngrp; ++grp) {
             const int buf = grp & 1, use = grp >> 1;
-            if (!mbar_wait_warp(&tfull[buf], (uint32_t)use & 1u, abort_flag)) {
+            if (!mbar_wait_warp(&tfull[buf], (uint32_t)use & 1u, abort_flag, flt.spin_limit)) {
                 ok = false;
                 break;
             }
@@ -343,9 +355,9 @@ __global__ void __launch_bounds__(TC_THREADS, DF ? 1 : 2)
     if (*abort_flag && threadIdx.x == 0) {
         atomicExch(err, 1);
         // drain: the MMAs in flight (accum) and the TMA loads issued but not consumed
-        mbar_wait(accum, 0, nullptr);
+        mbar_wait(accum, 0, nullptr, flt.spin_limit);
         for (int kb = *n_consumed; kb < *n_issued; ++kb)
-            mbar_wait(&full[kb % TC_STAGES], (uint32_t)(kb / TC_STAGES) & 1u, nullptr);
+            mbar_wait(&full[kb % TC_STAGES], (uint32_t)(kb / TC_STAGES) & 1u, nullptr, flt.spin_limit);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -370,7 +382,8 @@ inline int tc_ksplit_count(int64_t nk, int want) {
 // a multiple of 4 floats (16 bytes).
 template <class EPI, int FLUSH = 1, bool DF = false>
 int tc_gemm_tf32_mapped(cudaStream_t st, const TcOperand& A, const TcKMap& ka, const TcOperand& B, const TcKMap& kb,
-                        int64_t batch, int64_t lower_div, const EPI& epi, int* err, int ksplit = 1) {
+                        int64_t batch, int64_t lower_div, const EPI& epi, int* err, int ksplit = 1,
+                        TcFault flt = TcFault{}) {
     if (A.rows <= 0 || B.rows <= 0 || batch <= 0) return 0;
     if (FLUSH > 1 && (ksplit != 1 || ka.nkp % FLUSH || kb.nkp % FLUSH)) {
         set_error(FORGE_ERR_ARG, "tc_gemm: exact-block mode needs whole flush groups per segment and no K split");
@@ -405,7 +418,7 @@ int tc_gemm_tf32_mapped(cudaStream_t st, const TcOperand& A, const TcKMap& ka, c
     dim3 grd((unsigned)((A.rows + TC_BM - 1) / TC_BM), (unsigned)((B.rows + TC_BN - 1) / TC_BN),
              (unsigned)(batch * ks));
     k_tc_gemm_tf32<EPI, FLUSH, DF><<<grd, TC_THREADS, TC_SMEM, st>>>(ma, mb, A.rows, B.rows, ka, kb, lower_div, ks,
-                                                                     kchunk, epi, err);
+                                                                     kchunk, epi, err, flt);
     FORGE_LAUNCH_CHECK();
     return 0;
 }
@@ -413,13 +426,13 @@ int tc_gemm_tf32_mapped(cudaStream_t st, const TcOperand& A, const TcKMap& ka, c
 // Plain form: row-major A (M x K) and B (N x K), batch in the 3rd dimension.
 template <class EPI>
 int tc_gemm_tf32(cudaStream_t st, const TcOperand& A, const TcOperand& B, int64_t K, int64_t batch, const EPI& epi,
-                 int* err, int64_t lower_div = 0) {
+                 int* err, int64_t lower_div = 0, TcFault flt = TcFault{}) {
     TcOperand a = A, bb = B;
     a.cols = K;
     bb.cols = K;
     a.nplanes = batch;
     bb.nplanes = batch;
-    return tc_gemm_tf32_mapped(st, a, tc_kmap_plain(K), bb, tc_kmap_plain(K), batch, lower_div, epi, err);
+    return tc_gemm_tf32_mapped(st, a, tc_kmap_plain(K), bb, tc_kmap_plain(K), batch, lower_div, epi, err, 1, flt);
 }
 
 }  // namespace forge

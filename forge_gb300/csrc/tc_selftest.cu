@@ -20,8 +20,8 @@ struct StoreEpi {
 
 using namespace forge;
 
-extern "C" int forge_gpu_selftest_tc_gemm(int64_t M, int64_t N, int64_t K, int64_t batch, const float* A,
-                                          const float* B, float* D) {
+static int selftest_run(int64_t M, int64_t N, int64_t K, int64_t batch, const float* A, const float* B, float* D,
+                        TcFault flt) {
     if (M < 1 || N < 1 || K < 1 || batch < 1 || !A || !B || !D) {
         set_error(FORGE_ERR_ARG, "selftest_tc_gemm: bad arguments");
         return FORGE_ERR_ARG;
@@ -41,7 +41,7 @@ extern "C" int forge_gpu_selftest_tc_gemm(int64_t M, int64_t N, int64_t K, int64
     FORGE_CUDA(cudaMemcpy2DAsync(dB.ptr, ld * 4, B, K * 4, K * 4, batch * N, cudaMemcpyHostToDevice, st));
     TcOperand a{dA.as<float>(), M, K, ld, M * ld};
     TcOperand b{dB.as<float>(), N, K, ld, N * ld};
-    rc = tc_gemm_tf32(st, a, b, K, batch, StoreEpi{dD.as<float>(), N, M * N}, derr.as<int>());
+    rc = tc_gemm_tf32(st, a, b, K, batch, StoreEpi{dD.as<float>(), N, M * N}, derr.as<int>(), 0, flt);
     int herr = 0;
     if (!rc) {
         FORGE_CUDA(cudaMemcpyAsync(D, dD.ptr, batch * M * N * 4, cudaMemcpyDeviceToHost, st));
@@ -54,4 +54,24 @@ extern "C" int forge_gpu_selftest_tc_gemm(int64_t M, int64_t N, int64_t K, int64
         rc = FORGE_ERR_TIMEOUT;
     }
     return rc;
+}
+
+extern "C" int forge_gpu_selftest_tc_gemm(int64_t M, int64_t N, int64_t K, int64_t batch, const float* A,
+                                          const float* B, float* D) {
+    return selftest_run(M, N, K, batch, A, B, D, TcFault{});
+}
+
+// Failure detection without a fault: the producer stops after K block 0, so the MMA issuer's
+// bounded wait for block 1 runs out (spin_limit iterations); the kernel sets its error flag,
+// drains, frees its TMEM and returns, and the call reports FORGE_ERR_TIMEOUT.
+extern "C" int forge_gpu_selftest_tc_gemm_timeout(int64_t M, int64_t N, int64_t K, int64_t spin_limit,
+                                                  const float* A, const float* B, float* D) {
+    if (K <= 32 || spin_limit < 1 || spin_limit > (int64_t)TC_SPIN_LIMIT) {
+        set_error(FORGE_ERR_ARG, "selftest_tc_gemm_timeout: needs K > 32 and 1 <= spin_limit <= %u", TC_SPIN_LIMIT);
+        return FORGE_ERR_ARG;
+    }
+    TcFault f;
+    f.spin_limit = (uint32_t)spin_limit;
+    f.stop_loads_at = 1;
+    return selftest_run(M, N, K, 1, A, B, D, f);
 }

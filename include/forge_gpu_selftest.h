@@ -18,6 +18,13 @@ extern "C" {
 int forge_gpu_selftest_tc_gemm(int64_t M, int64_t N, int64_t K, int64_t batch, const float* A, const float* B,
                                float* D);
 
+/* The same GEMM (batch 1) with a failure injected: the TMA producer issues only K block 0, so the
+ * MMA issuer's wait for block 1 runs out after spin_limit polls (1..2^26); the kernel flags the
+ * error, drains its copies and MMAs, frees its TMEM and returns.  Returns FORGE_ERR_TIMEOUT; the
+ * context stays usable.  K must exceed 32. */
+int forge_gpu_selftest_tc_gemm_timeout(int64_t M, int64_t N, int64_t K, int64_t spin_limit, const float* A,
+                                       const float* B, float* D);
+
 /* Host only: the small dense step of the window refinement.  G, S: n x n Hermitian (complex,
  * column-major, interleaved re/im doubles), n <= 32.  Returns theta (ascending) and M = L^{-H} U,
  * with S = L L^H and L^{-1} G L^{-H} = U diag(theta) U^H, so that G M = S M diag(theta) and

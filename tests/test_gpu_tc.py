@@ -66,3 +66,18 @@ def test_tc_gemm_accumulation_bias_is_bounded(lib):
         ref = A[0].astype(np.float64) @ B[0].astype(np.float64).T
         rel = (D[0] - ref) / np.abs(ref).max()
         assert abs(float(rel.mean())) <= 3e-7, (K, float(rel.mean()))
+
+
+def test_tc_gemm_bounded_wait_times_out_cleanly(lib):
+    """Failure detection without a GPU fault: a GEMM whose second K block never arrives gives up its
+    bounded mbarrier wait and returns FORGE_ERR_TIMEOUT (-5); the context then runs an exact GEMM."""
+    rng = np.random.default_rng(5)
+    A = rng.integers(-8, 9, size=(1, 256, 128)).astype(np.float32)
+    B = rng.integers(-8, 9, size=(1, 192, 128)).astype(np.float32)
+    D = np.zeros((1, 256, 192), np.float32)
+    rc = lib.forge_gpu_selftest_tc_gemm_timeout(256, 192, 128, 1 << 14, A.ctypes.data_as(C.c_void_p),
+                                                B.ctypes.data_as(C.c_void_p), D.ctypes.data_as(C.c_void_p))
+    assert rc == -5, lib.forge_gpu_last_error()
+    assert b"gave up" in lib.forge_gpu_last_error()
+    D2 = _tc(lib, A, B)
+    assert np.array_equal(D2[0].astype(np.float64), A[0].astype(np.float64) @ B[0].astype(np.float64).T)
