@@ -92,6 +92,7 @@ SIGNATURES = {
     "forge_gpu_field_guess": [_P, _P, _P, _P],
     "forge_gpu_scf_iteration": [_P, _P, _P],
     "forge_gpu_solve_group": [_P, _I, _P],
+    "forge_gpu_set_potential": [_P, _P],
     "forge_gpu_scf_iteration_group": [_P, _I, _P, _P],
     "forge_gpu_set_precision": [_P, _I],
     "forge_gpu_set_mixing": [_P, _I, _I, C.c_double],
@@ -449,6 +450,10 @@ class HartreeFock:
         info = _check(self.lib.forge_gpu_solve(self.ctx, _ptr(V), _ptr(P), _ptr(B), _ptr(E), _ptr(FB)),
                       allow_info=True)
         return B, E, FB, info
+
+    def SetPotential(self, Potential):
+        """Loads the potential of the next solve (for SolveGroup over several contexts)."""
+        _check(self.lib.forge_gpu_set_potential(self.ctx, _ptr(_f(Potential, np.float64))))
 
     def GetBands(self) -> np.ndarray:
         """Bands (numb, Nk) of the last solve (the window eigenvalues nLower..nUpper per k)."""

@@ -750,8 +750,24 @@ int sort_device(forge_ctx* x, double nfilling) {
     return 0;
 }
 
+// the bulk projector of bands 1..nLower-1 when the last solve left it out (the fused SCF iteration
+// and the group solve fold it into P_new instead)
+int ensure_bulk(forge_ctx* x) {
+    if (!x->bulk_is_fused) return 0;
+    Context& c = x->c;
+    FORGE_TRY(c.bulk.ensure(4 * (size_t)c.N * c.N * sizeof(double2)));
+    FORGE_CUDA(cudaMemsetAsync(c.bulk.ptr, 0, 4 * (size_t)c.N * c.N * sizeof(double2), c.stream));
+    if (x->tcerr.ptr) FORGE_CUDA(cudaMemsetAsync(x->tcerr.ptr, 0, sizeof(int), c.stream));
+    const int64_t kb = x->k_begin, ke = (x->k_end > 0) ? x->k_end : c.Nk;
+    for (int64_t k = kb; k < ke; ++k)
+        FORGE_TRY(project_k_c3(x, k, c.nLower - 1, &x->h_bph[k * 4], c.bulk.as<double2>()));
+    x->bulk_is_fused = false;
+    return 0;
+}
+
 int get_fock_device(forge_ctx* x, int64_t nstates) {
     Context& c = x->c;
+    FORGE_TRY(ensure_bulk(x));
     const size_t NN = (size_t)c.N * c.N;
     FORGE_TRY(x->Pn.ensure(4 * NN * sizeof(double2)));
     FORGE_CUDA(cudaMemsetAsync(x->Pn.ptr, 0, 4 * NN * sizeof(double2), c.stream));
@@ -1773,6 +1789,7 @@ int forge_gpu_get_fock(forge_ctx* x, double DegFactor, int64_t nOccStates, int64
     if (x->valley) {
         // Main.f90:470-511: the averaged window plus zFockBulk, divided by Nk
         const size_t NN = (size_t)c.N * c.N;
+        FORGE_TRY(ensure_bulk(x));
         FORGE_TRY(x->Pn.ensure(4 * NN * sizeof(double2)));
         FORGE_CUDA(cudaMemsetAsync(x->Pn.ptr, 0, 4 * NN * sizeof(double2), c.stream));
         FORGE_TRY(valley_window(x, st));
@@ -1963,6 +1980,17 @@ int forge_gpu_prepare_state(forge_ctx* x, double* Energies) {
     Context& c = x->c;
     if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
     return prepare_state_device(x, Energies);
+}
+
+int forge_gpu_set_potential(forge_ctx* x, const double* Potential) {
+    FORGE_TRY(check_ctx(x));
+    if (!Potential) {
+        set_error(FORGE_ERR_ARG, "set_potential: null Potential");
+        return FORGE_ERR_ARG;
+    }
+    FORGE_TRY(upload_state(x, Potential, nullptr));
+    FORGE_CUDA(cudaStreamSynchronize(x->c.stream));
+    return 0;
 }
 
 int forge_gpu_solve_group(forge_ctx** ctxs, int64_t nctx, int64_t* info) {

@@ -11,8 +11,9 @@ host joins the spins:
 - it takes one OptimalStep for both spins;
 - it builds each spin's potential from both densities (Main.f90:586-594).
 
-Density matrices cross the host boundary once per energy evaluation.  This path is for correctness
-and for systems of moderate size; it is not the benchmarked path.
+The two spins' eigen-solves share one batched launch sequence (forge_gpu_solve_group over the two
+contexts).  Density matrices cross the host boundary once per energy evaluation.  This path is for
+correctness and for systems of moderate size; it is not the benchmarked path.
 
 Arrays follow the reference: zFock(ndim, ndim, numNeighborCells) per spin, column-major.
 """
@@ -25,8 +26,8 @@ import numpy as np
 
 import os
 
-from .api import (Geometry, HartreeFock, Setup, build_geometry, fermi_2spins, parameters_string, plot_bands, read_fock,
-                  write_fock)
+from .api import (Geometry, HartreeFock, Setup, SolveGroup, build_geometry, fermi_2spins, parameters_string,
+                  plot_bands, read_fock, write_fock)
 
 
 @dataclasses.dataclass
@@ -157,10 +158,20 @@ class SpinPolarisedScf:
             raise RuntimeError("no state: call plain_guess() or set_state() first")
         s = self.s
         sorted_e = []
+        if all(isinstance(h, HartreeFock) for h in self.hf) and not self.setup.nenforceC3 \
+                and not self.setup.nenforceValley:
+            # both spins' H(k) in one batched eigen-solve (the device group solve)
+            for sp in range(2):
+                self.hf[sp].SetPotential(self.V[sp])
+            info = SolveGroup(self.hf)
+            if np.any(info > 0):
+                print("zheev failed", int(np.sum(info)))   # LapackRoutines.f90:430 behaviour
+        else:
+            for sp in range(2):
+                _, _, _, info = self.hf[sp].Solve(self.V[sp], None, bands=False)
+                if info > 0:
+                    print("zheev failed", info)           # LapackRoutines.f90:430 behaviour
         for sp in range(2):
-            _, _, _, info = self.hf[sp].Solve(self.V[sp], None, bands=False)
-            if info > 0:
-                print("zheev failed", info)           # LapackRoutines.f90:430 behaviour
             e, _, _ = self.hf[sp].SortEnergies_1Spin()
             sorted_e.append(e)
         fl = fermi_2spins(self.setup, np.stack(sorted_e, 1))

@@ -204,6 +204,10 @@ int forge_gpu_scf_iteration(forge_ctx* ctx, double* Energies, forge_iter_report*
  * mixed precision).  info[b] (NULL allowed): number of k of context b whose solve did not converge.
  * The work runs on ctxs[0]'s stream and its group buffers. */
 int forge_gpu_solve_group(forge_ctx** ctxs, int64_t nctx, int64_t* info);
+/* Loads Potential (ndim) as the potential of the next solve without solving (the Potential argument
+ * of Solve, HartreeFock.f90:402-411, for hosts that batch several contexts' solves with
+ * forge_gpu_solve_group, e.g. the two spins of numS = 2). */
+int forge_gpu_set_potential(forge_ctx* ctx, const double* Potential);
 /* One SCF iteration of each context (forge_gpu_scf_iteration) with the eigen-solve shared as in
  * forge_gpu_solve_group: Energies is nctx x 4 (NULL allowed), reports nctx (NULL allowed). */
 int forge_gpu_scf_iteration_group(forge_ctx** ctxs, int64_t nctx, double* Energies, forge_iter_report* reports);
