@@ -409,6 +409,8 @@ def main():
     ap.add_argument("--ref-n-max", type=int, default=1 << 30,
                     help="reference arm: largest principal block timed (default: the full N)")
     ap.add_argument("--c3", action="store_true")
+    ap.add_argument("--numk", type=int, default=0,
+                    help="profiling cases only: override the workload's k grid (numk x numk)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -419,6 +421,9 @@ def main():
         args.no_cpu_baseline = True
         args.budget_s = max(args.budget_s, 1e9)
     cfg = dict(CONFIGS[args.config])
+    if args.numk > 0:
+        cfg["numk"] = args.numk
+        cfg["name"] += f"_k{args.numk}x{args.numk}"
     if args.c3:
         if cfg["numk"] % 3:
             ap.error("--c3 needs a k grid with numk divisible by 3")
