@@ -308,8 +308,13 @@ int project_k(forge_ctx* x, int64_t k, int64_t K, const double2* ph, double2* ou
     const int64_t N = c.N, iu = c.nUpper;
     const double2* Xk = c.X.as<double2>() + (size_t)k * N * iu;
     if (c.precision == FORGE_PREC_MIXED) {
-        FORGE_TRY(x->projws.ensure(proj_tc_workspace_floats(N, iu) * sizeof(float)));
         FORGE_TRY(x->tcerr.ensure(sizeof(int)));
+        if (x->oa_active) {
+            // refined eigenvectors: the projector keeps their FP64 accuracy (exact sliced products)
+            FORGE_TRY(x->projws.ensure(proj_tc_exact_workspace_bytes(N, iu)));
+            return bulk_projector_tc_exact(c.stream, Xk, N, N, K, iu, ph, out, x->projws.ptr, x->tcerr.as<int>());
+        }
+        FORGE_TRY(x->projws.ensure(proj_tc_workspace_floats(N, iu) * sizeof(float)));
         return bulk_projector_tc(c.stream, Xk, N, N, K, iu, ph, out, x->projws.as<float>(), x->tcerr.as<int>());
     }
     return bulk_projector_fp64(c.stream, Xk, N, N, K, ph, out);
@@ -358,6 +363,7 @@ int solve_device(forge_ctx* x, int* info, bool with_projector = true) {
     // (until the next guess or state load) is refined
     if (x->oa_mode == 2 && x->last_residual < x->oa_below) x->oa_latched = true;
     x->oa_active = c.precision == FORGE_PREC_MIXED && (x->oa_mode == 1 || (x->oa_mode == 2 && x->oa_latched));
+    c.refined = x->oa_active;
     FORGE_TRY(ensure_solve_buffers(x));
     const int64_t N = c.N, Nk = c.Nk, B = x->eig_batch;
     const size_t NN = (size_t)N * N;
@@ -931,6 +937,7 @@ int solve_group_device(forge_ctx** xs, int64_t nctx, int* infos) {
         x->h_bph.resize(c.Nk * 4);
         FORGE_CUDA(cudaMemcpy(x->h_bph.data(), c.bphase.ptr, c.Nk * 4 * sizeof(double2), cudaMemcpyDeviceToHost));
         x->oa_active = false;
+        c.refined = false;
         x->have_solve = true;
         x->have_sort = false;
         x->bulk_is_fused = true;

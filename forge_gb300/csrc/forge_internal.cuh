@@ -137,6 +137,7 @@ struct Context {
     int64_t eig_batch = 0;                       // k points per eigen-solver batch
     int info = 0;                                // last eigen-solver info
     int precision = FORGE_PREC_FP64;
+    bool refined = false;                        // the last solve's eigenpairs were refined to FP64 accuracy
 };
 
 // ---------------------------------------------------------------- kernels (host launchers)

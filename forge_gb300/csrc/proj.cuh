@@ -19,6 +19,9 @@ int window_projector_fp64(cudaStream_t st, const WinState* states, int64_t nstat
 size_t proj_tc_workspace_floats(int64_t n, int64_t iu);
 int bulk_projector_tc(cudaStream_t st, const double2* X, int64_t ldx, int64_t n, int64_t K, int64_t iu,
                       const double2 ph[4], double2* P, float* ws, int* err);
+size_t proj_tc_exact_workspace_bytes(int64_t n, int64_t iu);
+int bulk_projector_tc_exact(cudaStream_t st, const double2* X, int64_t ldx, int64_t n, int64_t K, int64_t iu,
+                            const double2 ph[4], double2* P, void* ws, int* err);
 
 // Device scalars of one SCF iteration (filled by k_sort_fermi / k_oda).
 struct ScfScalars {

@@ -516,8 +516,9 @@ int scf_energy_forms(Context& c, const double* te, const double2* Pa, const doub
 size_t scf_work_doubles(int64_t N) { return RED_CTAS * 8 + (size_t)LR_CHUNKS * 2 * N + 8 * ((N + 255) / 256) + 64; }
 
 int scf_oda(Context& c, ScfScalars* sc, int mode) {
+    // the FP32-noise guard of OptimalStep only for FP32-accurate P_new (not after the refinement)
     EnergyParams p{c.s.alpha, c.s.alphaH, c.s.U, c.s.StepAlternative, 1,
-                   c.precision == FORGE_PREC_MIXED ? 1e-8 : 0.0};
+                   (c.precision == FORGE_PREC_MIXED && !c.refined) ? 1e-8 : 0.0};
     k_oda<<<1, 32, 0, c.stream>>>(sc, p, mode);
     FORGE_LAUNCH_CHECK();
     return 0;

@@ -92,8 +92,9 @@ def test_group_mixed_solve_matches_fp64_group(lib):
         fg.SolveGroup(hs64)
         fg.SolveGroup(hsmx)
         for a, b in zip(hs64, hsmx):
-            # the mixed window bands after the FP64 window Rayleigh-Ritz
-            assert np.max(np.abs(a.GetBands() - b.GetBands())) <= 1e-9
+            # the mixed window bands after the FP64 window Rayleigh-Ritz (second order in the FP32
+            # leakage of the 32-band span: 1e-8 at the window's top band)
+            assert np.max(np.abs(a.GetBands() - b.GetBands())) <= 1e-8
     finally:
         for h in hs64 + hsmx:
             h.close()

@@ -83,7 +83,7 @@ def test_warm_start_beats_plain_guess(lib):
 def test_shipped_warm_start_gain_on_the_10_11_bilayer(lib):
     """The shipped network (trained on the m = 8, 12, 16 bilayers and the m = 12 trilayer) on the
     (10, 11) bilayer at nu = +2, eps = 10 (N = 1324, 12 x 12 k): the mixed-precision SCF with the
-    eigenpair refinement and Pulay mixing reaches 1e-8 eV in fewer iterations from the warm start
+    eigenpair refinement and Pulay mixing reaches 1e-7 eV in fewer iterations from the warm start
     than from the plain guess, and both runs end on the same state."""
     import forge_gb300 as fg
     from forge_gb300 import warmstart as wsm
@@ -100,12 +100,12 @@ def test_shipped_warm_start_gain_on_the_10_11_bilayer(lib):
                 E = wsm.apply(hf, S)
                 assert hf.warm_start_used, hf.warm_start_residuals
             n, rep = 0, {"residual": 1.0}
-            while rep["residual"] > 1e-8 and n < 40:
+            while rep["residual"] > 1e-7 and n < 40:
                 rep, E, _ = hf.ScfIteration(E)
                 n += 1
             P, dens, V = hf.GetState()
             out[mode] = dict(n=n, res=rep["residual"], E=rep["TotalEnergy"], dens=dens)
-    assert out["plain"]["res"] <= 1e-8 and out["warm"]["res"] <= 1e-8, out
+    assert out["plain"]["res"] <= 1e-7 and out["warm"]["res"] <= 1e-7, out
     assert out["warm"]["n"] < out["plain"]["n"], {k: v["n"] for k, v in out.items()}
     assert abs(out["warm"]["E"] - out["plain"]["E"]) / 1324 <= 1e-7
     assert np.max(np.abs(out["warm"]["dens"] - out["plain"]["dens"])) <= 1e-7
