@@ -98,6 +98,7 @@ SIGNATURES = {
     "forge_gpu_set_mixing": [_P, _I, _I, C.c_double],
     "forge_gpu_set_refinement": [_P, _I],
     "forge_gpu_set_eigen_refinement": [_P, _I, _D, _D, _I],
+    "forge_gpu_last_refined": [_P, _P],
     "forge_selftest_rr_small": [_I, _P, _P, _P, _P],
     "forge_gpu_get_setup": [_P, _P],
     "forge_gpu_synchronize": [_P],
@@ -377,6 +378,12 @@ class HartreeFock:
         """Eigenpair refinement of the mixed solve: 0 off, 1 every mixed solve, 2 once the SCF residual
         is below residual_below (eV); delta (eV) and depth 0 = defaults (1e-3, 4)."""
         _check(self.lib.forge_gpu_set_eigen_refinement(self.ctx, mode, residual_below, delta, depth))
+
+    def last_solve_refined(self) -> int:
+        """1 if the last solve's eigenpairs were refined (forge_gpu_set_eigen_refinement)."""
+        r = C.c_int64()
+        _check(self.lib.forge_gpu_last_refined(self.ctx, C.byref(r)))
+        return int(r.value)
 
     def set_c3(self, nenforceC3: int = 1):
         """nenforceC3 (Setup.f90:27): 1 = Solve_C3 / GetFock_C3, 0 = the full solve."""

@@ -1199,6 +1199,12 @@ int forge_gpu_set_eigen_refinement(forge_ctx* x, int64_t mode, double residual_b
     return 0;
 }
 
+int forge_gpu_last_refined(forge_ctx* x, int64_t* refined) {
+    FORGE_TRY(check_ctx(x));
+    if (refined) *refined = x->oa_active ? 1 : 0;
+    return 0;
+}
+
 int forge_gpu_set_c3(forge_ctx* x, int64_t nenforceC3, const int64_t* nC3pairs, const int64_t* RotateLayers) {
     FORGE_TRY(check_ctx(x));
     Context& c = x->c;

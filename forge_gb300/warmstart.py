@@ -15,9 +15,10 @@ vectors at the site or bond centre: the local stacking registry), plus sublattic
 bond vector, filling nu and 1/epsilon, so they transfer between twist angles.
 
 The predicted field is diagonalised once (the cost of the plain guess) to give the starting
-density matrix.  If the predicted field is further from the field of that density matrix than
-the zero field is (i.e. the network's first residual is worse than the plain guess's), the
-plain guess is used instead.
+density matrix.  `start` then applies the fallback rule: the first SCF iteration runs from the
+network's state and from the plain guess, and the SCF continues from the plain guess whenever
+the network's first residual is worse (the price is one guess and one iteration of the loser).
+`apply` alone is the cheaper form that compares the predicted field with the zero field.
 """
 from __future__ import annotations
 
@@ -238,9 +239,45 @@ def predicted_state(hf: HartreeFock, ws: WarmStart) -> np.ndarray:
     return P
 
 
-def apply(hf: HartreeFock, setup: Setup, ws: Optional[WarmStart] = None, path: str = WEIGHTS):
-    """Starting guess for `hf` from the network; returns the initial energies (4).  Falls back to
-    the plain guess when the predicted field's residual is not better than the zero field's."""
+def start(hf: HartreeFock, setup: Setup, ws: Optional[WarmStart] = None, path: str = WEIGHTS):
+    """The learned start with the fallback rule: the SCF starts from the network's field unless the
+    network's first residual is worse than the plain guess's.
+
+    Both starts run their first SCF iteration: the network's field (forge_gpu_field_guess, one
+    diagonalisation) and then the plain guess (Main.f90:236-346).  The first iteration's residual of
+    each is compared; the plain run continues in place when it is not worse, otherwise the network
+    run's state after its first iteration is restored.  Returns (energies after the first iteration,
+    that iteration's report, info).  info["first_residuals"] = (network, plain)."""
+    E_w = apply(hf, setup, ws, path, fallback=False)
+    used = bool(hf.warm_start_used)
+    info = {"field_residuals": list(hf.warm_start_residuals)}
+    if used:
+        rep_w, E_w1, _ = hf.ScfIteration(E_w)
+        P_w, _, _ = hf.GetState()
+        r_w = rep_w["residual"]
+    else:
+        r_w = float("nan")
+    E_p, _ = hf.PlainGuess()
+    rep_p, E_p1, _ = hf.ScfIteration(E_p)
+    r_p = rep_p["residual"]
+    info["first_residuals"] = [r_w, r_p]
+    if used and r_w < r_p:
+        hf.SetState(P_w)
+        E = hf.PrepareState()
+        hf.warm_start_used = True
+        info["warm_start_used"] = True
+        return tuple(E), rep_w, info
+    hf.warm_start_used = False
+    info["warm_start_used"] = False
+    return tuple(E_p1), rep_p, info
+
+
+def apply(hf: HartreeFock, setup: Setup, ws: Optional[WarmStart] = None, path: str = WEIGHTS,
+          fallback: bool = True):
+    """Starting guess for `hf` from the network's field (one diagonalisation); returns the initial
+    energies (4).  A non-finite prediction is never used (plain guess).  With `fallback`, the plain
+    guess is also taken when the predicted field's residual (against the field of the state it
+    gives) is not below the zero field's; `start` applies the first-iteration rule instead."""
     if ws is None:
         if not os.path.exists(path):
             raise ForgeError(-1, f"warm-start weights not found at {path}")
@@ -257,7 +294,7 @@ def apply(hf: HartreeFock, setup: Setup, ws: Optional[WarmStart] = None, path: s
     rc = hf.lib.forge_gpu_field_guess(hf.ctx, _ptr(np.asfortranarray(P)), _ptr(E), _ptr(res))
     _check(rc, allow_info=True)
     hf.warm_start_residuals = (float(res[0]), float(res[1]))
-    if not (res[0] < res[1]):          # also when a residual is NaN
+    if not np.isfinite(res[0]) or (fallback and not (res[0] < res[1])):
         E2, _ = hf.PlainGuess()
         hf.warm_start_used = False
         return tuple(E2)

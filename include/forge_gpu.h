@@ -240,6 +240,8 @@ int forge_gpu_set_refinement(forge_ctx* ctx, int64_t width);
  * slice products s + t <= depth, relative accuracy of the residual ~2^-(25 + 9 depth). */
 int forge_gpu_set_eigen_refinement(forge_ctx* ctx, int64_t mode, double residual_below, double delta,
                                    int64_t depth);
+/* 1 if the last solve's eigenpairs were refined (for hosts that call forge_gpu_solve directly). */
+int forge_gpu_last_refined(forge_ctx* ctx, int64_t* refined);
 
 /* nenforceC3 (Setup.f90:27): 1 selects Solve_C3 / GetFock_C3 (HartreeFock.f90:131-398, 564-881) in
  * every later solve and projector; 0 (the default) the full solve.  nC3pairs is the 1-based site map
