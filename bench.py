@@ -153,8 +153,9 @@ def _make(args, cfg):
     if mixed:
         hf.set_refinement(args.rr_width)
         if not args.no_oa:
-            # the eigenpair refinement once the SCF is within reach of the tolerance (latched)
-            hf.set_eigen_refinement(2, args.oa_below, 0.0, args.oa_depth)
+            # the eigenpair refinement once the SCF is within reach of the tolerance (latched), or
+            # on every solve (--oa-always: the FP64-equivalent trajectory)
+            hf.set_eigen_refinement(1 if args.oa_always else 2, args.oa_below, 0.0, args.oa_depth)
     hf.LongRangeInteraction(copy_out=False)
     hf.synchronize()
     return S, hf
@@ -444,6 +445,7 @@ def main():
     ap.add_argument("--oa-stall", type=float, default=1e-3,
                     help="mixed modes: refine every later solve once the residual stalls below this (eV)")
     ap.add_argument("--oa-depth", type=int, default=4)
+    ap.add_argument("--oa-always", action="store_true", help="mixed modes: refine every solve")
     ap.add_argument("--ref-n-max", type=int, default=1 << 30,
                     help="reference arm: largest principal block timed (default: the full N)")
     ap.add_argument("--c3", action="store_true")

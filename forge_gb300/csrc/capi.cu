@@ -142,6 +142,7 @@ struct forge_ctx {
 namespace {
 
 int read_scalars(forge_ctx* x, ScfScalars* h);
+void diis_reset(forge_ctx* x);
 
 int check_ctx(forge_ctx* x) {
     if (!x) {
@@ -362,8 +363,12 @@ int solve_device(forge_ctx* x, int* info, bool with_projector = true) {
     // mode 2 latches: once an SCF residual fell below oa_below, every later solve of that SCF
     // (until the next guess or state load) is refined
     if (x->oa_mode == 2 && x->last_residual < x->oa_below) x->oa_latched = true;
+    const bool was_active = x->oa_active;
     x->oa_active = c.precision == FORGE_PREC_MIXED && (x->oa_mode == 1 || (x->oa_mode == 2 && x->oa_latched));
     c.refined = x->oa_active;
+    // the Pulay history of FP32-accurate iterations holds their noise: the refined iterations start
+    // a new one (as a change of precision does)
+    if (x->oa_active && !was_active) diis_reset(x);
     FORGE_TRY(ensure_solve_buffers(x));
     const int64_t N = c.N, Nk = c.Nk, B = x->eig_batch;
     const size_t NN = (size_t)N * N;
