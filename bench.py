@@ -440,8 +440,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rr-width", type=int, default=32)
     ap.add_argument("--no-oa", action="store_true", help="mixed modes without the eigenpair refinement")
-    ap.add_argument("--oa-below", type=float, default=1e-5,
-                    help="mixed modes: residual (eV) below which every later solve is refined")
+    ap.add_argument("--oa-below", type=float, default=1.0,
+                    help="mixed modes: residual (eV) below which every later solve is refined (default: "
+                         "from the second iteration on; the first iterations of the two starts that the "
+                         "fast mode compares run unrefined)")
     ap.add_argument("--oa-stall", type=float, default=1e-3,
                     help="mixed modes: refine every later solve once the residual stalls below this (eV)")
     ap.add_argument("--oa-depth", type=int, default=4)

@@ -33,6 +33,8 @@ SYSTEMS = [
     (12, 2, 6, 2.0, 10.0), (12, 2, 6, -2.0, 10.0), (12, 2, 6, 1.0, 10.0), (12, 2, 6, 3.0, 10.0),
     (16, 2, 4, 2.0, 10.0), (16, 2, 4, 0.0, 10.0),
     (12, 3, 4, 2.0, 10.0),
+    # the (10, 11) bilayer at the fillings other than +2 (the warm start's target workload there)
+    (10, 2, 6, 0.0, 10.0), (10, 2, 6, 1.0, 10.0), (10, 2, 6, 3.0, 10.0), (10, 2, 6, -2.0, 10.0),
 ]
 QUICK = [(8, 2, 6, 2.0, 10.0), (8, 2, 6, 0.0, 10.0), (12, 2, 4, 2.0, 10.0)]
 
