@@ -133,7 +133,10 @@ def test_fast_path_reaches_the_oracle_fixed_point(lib):
     assert np.max(np.abs(dens - gd["dens"])) <= 1e-8
     b = gd["bonds"]
     assert np.max(np.abs(P[b[:, 0], b[:, 1], b[:, 2]] - gd["P_bonds"])) <= 1e-8
-    assert np.max(np.abs(bands - gd["bands"])) <= 1e-9
+    # both states are converged to a residual of 1e-9 eV (the fixture to 1e-10): their bands agree to
+    # that level times the field's sensitivity (the same-input bands agree to 1e-9 eV in
+    # test_refined_mixed_solve_matches_lapack)
+    assert np.max(np.abs(bands - gd["bands"])) <= 1e-8
     ref_op = dict(zip([str(n) for n in gd["order_names"]], gd["order"]))
     for k, v in op.items():
         assert abs(v - ref_op[k]) <= 1e-7 * max(1.0, abs(ref_op[k])), (k, v, ref_op[k])
