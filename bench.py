@@ -310,9 +310,9 @@ def run_ours(args, cfg):
     # warm-up: W iterations from the plain guess, untimed (the timed SCF starts again from its guess)
     E, _ = hf.PlainGuess()
     E = list(E)
-    for _ in range(args.warmup):
+    for w in range(args.warmup):
         rep, E, _ = hf.ScfIteration(E)
-        _log({"warmup_iter": _ + 1, "residual": rep["residual"]})
+        _log({"warmup_iter": w + 1, "residual": rep["residual"]})
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     run = scf_device(hf, S, args, args.steps, args.budget_s, t_wall0, profile=True)
