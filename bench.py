@@ -73,13 +73,55 @@ PLAIN_FP64_RECORDED = {
         "command": "python bench.py --config 1 --mode plain --converge"},
 }
 
-# DRAM traffic of the dominant kernels per algorithmic byte, from ncu captures small enough for the
-# profiler (dram__bytes_read.sum + dram__bytes_write.sum over the work model's bytes).
+# DRAM traffic of the dominant kernels from ncu captures small enough for the profiler
+# (dram__bytes_read.sum + dram__bytes_write.sum), per unit of the work model: per algorithmic byte
+# for the streaming kernels, per algorithmic flop for the sliced residual product (its DRAM bytes
+# are panel re-reads, which grow with the tile-K products, i.e. with the flops, not with the
+# operand bytes).
 NCU_TRAFFIC_RATIO = {
-    "hemv": (1.044, "ncu --set full of k_trd_hemv<float> at N=5044, column 1501 (n'=3543): 52.25 MB read + "
-                    "0.19 MB written against 50.23 MB algorithmic (trailing lower triangle, complex64); "
-                    "python -m forge_gb300.eigbench --m 20 --precision mixed"),
+    "hemv": (1.044, "bytes", "ncu --set full of k_trd_hemv<float> at N=5044, column 1501 (n'=3543): 52.25 MB "
+                             "read + 0.19 MB written against 50.23 MB algorithmic (trailing lower triangle, "
+                             "complex64); python -m forge_gb300.eigbench --m 20 --precision mixed"),
+    "oa_gemm": (0.01628, "flops", "ncu (SpeedOfLight, MemoryWorkloadAnalysis) of k_tc_gemm_tf32<OaWEpi, 8, 1> at "
+                                  "N=5044, iu=2532, depth 4: 2.528 TB/s x 24.89 ms = 62.9 GB for one launch of "
+                                  "3.865e12 slice-product flop; python bench.py --config 2 --numk 2 --mode mixed "
+                                  "--oa-always --steps 1 --warmup 3 --no-e2e --no-cpu-baseline"),
 }
+
+
+ROOFED = {"assemble", "hemv", "her2k", "backtransform", "projector", "window", "energy", "lr_matvec", "mix",
+          "refine", "oa_gemm"}
+TENSOR_STAGES = {"her2k", "backtransform", "projector", "window", "oa_gemm"}
+
+
+def roofline(kernels, mode, peaks):
+    """The roofline object of the dominant stage with a throughput bound.  kernels: the library
+    profiler's per-stage totals ({stage: {"ms", "launches", "bytes", "flops"}}, launches > 0);
+    peaks: (hbm GB/s, bf16 TFLOP/s, source)."""
+    hbm, bf16, src = peaks
+    cand = [k for k in kernels if k in ROOFED]
+    if not cand:
+        return None
+    dom = max(cand, key=lambda k: kernels[k]["ms"])
+    d = kernels[dom]
+    per_launch_ms = d["ms"] / d["launches"]
+    if mode != "plain" and dom in TENSOR_STAGES:
+        ach = d["flops"] / d["launches"] / (per_launch_ms * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16}
+    else:
+        ach = d["bytes"] / d["launches"] / (per_launch_ms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm}
+    alg = d["bytes"] / d["launches"]
+    tr = NCU_TRAFFIC_RATIO.get(dom)
+    units = (d["flops"] if tr and tr[1] == "flops" else d["bytes"]) / d["launches"]
+    roof.update({"kernel": dom, "launches": d["launches"], "avg_launch_ms": per_launch_ms,
+                 "algorithmic_bytes_per_launch": alg, "algorithmic_flops_per_launch": d["flops"] / d["launches"],
+                 "peak_source": f"{src} (MEASURED_PEAKS.json)" if src == "measured" else src,
+                 "traffic": tr[0] * units if tr else None,
+                 "traffic_source": f"{tr[2]}; ratio {tr[0]} B per algorithmic {tr[1][:-1]} x this run's "
+                                   f"algorithmic {tr[1]} per launch (scaled from the small capture)" if tr
+                 else None})
+    return roof
 
 
 def _peaks():
@@ -412,6 +454,15 @@ def _cpu_k_point(fo, so, coords, u1, u2, t1, t2, vk, n_max):
     return dict(t_iter=t_iter, cores=cores, parts=parts, measured=measured, sample=how, full=(Ns == N))
 
 
+def _iterations_source(rec):
+    if not rec:
+        return "no plain FP64 record for this workload: value is null, ms_per_step is measured"
+    kind = ("iteration count of the FP64-equivalent SCF trajectory (every mixed solve refined to FP64 "
+            "accuracy), with the same mixer" if rec.get("estimated") else
+            "measured iteration count of the plain FP64 GPU SCF with the same mixer")
+    return f"{kind} ({rec['command']}, {rec['date']}); the time per iteration is this run's"
+
+
 def run_reference(args, cfg):
     """The reference arm: the oracle port (the reference's CPU algorithm restated; the Fortran
     reference cannot be built here) on the host cores, one full-size k point, no GPU library."""
@@ -501,10 +552,7 @@ def main():
                 "impl": "reference", "dtype": "f64", "data": "synthetic",
                 "config": {"workload": cfg["name"], "iters": r["iters"], "cpu_parts_s": cs["parts"],
                            "measured_s": cs["measured"], "geometry_s": r["t_geo"],
-                           "iterations_source": ("measured iteration count of the plain FP64 GPU SCF with the same "
-                                                 f"mixer ({r['rec']['command']}, {r['rec']['date']}); the "
-                                                 "time per iteration is this run's") if r["rec"] else
-                           "no plain FP64 record for this workload: value is null, ms_per_step is measured"},
+                           "iterations_source": _iterations_source(r["rec"])},
                 "cpu_baseline": {"value": val, "unit": "s", "cores": cs["cores"], "kind": "port",
                                  "sample": cs["sample"]},
                 "e2e": {"value": val, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -537,31 +585,9 @@ def main():
         t_e2e = float(t[2]) if t_e2e is not None else None
     if rank != 0:
         return
-    hbm, bf16, src = _peaks()
     prof = run.get("prof", {})
     kernels = {k: v for k, v in prof.items() if v["launches"] > 0}
-    roofed = {"assemble", "hemv", "her2k", "backtransform", "projector", "window", "energy", "lr_matvec", "mix",
-              "refine", "oa_gemm"}
-    roof = None
-    if any(k in roofed for k in kernels):
-        dom = max((k for k in kernels if k in roofed), key=lambda k: kernels[k]["ms"])
-        d = kernels[dom]
-        per_launch_ms = d["ms"] / d["launches"]
-        tensor_stages = {"her2k", "backtransform", "projector", "window", "oa_gemm"}
-        if args.mode != "plain" and dom in tensor_stages:
-            ach = d["flops"] / d["launches"] / (per_launch_ms * 1e-3) / 1e12
-            roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16}
-        else:
-            ach = d["bytes"] / d["launches"] / (per_launch_ms * 1e-3) / 1e9
-            roof = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm}
-        alg = d["bytes"] / d["launches"]
-        tr = NCU_TRAFFIC_RATIO.get(dom)
-        roof.update({"kernel": dom, "launches": d["launches"], "avg_launch_ms": per_launch_ms,
-                     "algorithmic_bytes_per_launch": alg, "algorithmic_flops_per_launch": d["flops"] / d["launches"],
-                     "peak_source": f"{src} (MEASURED_PEAKS.json)" if src == "measured" else src,
-                     "traffic": tr[0] * alg if tr else None,
-                     "traffic_source": f"{tr[1]}; ratio {tr[0]} x this run's algorithmic bytes per launch" if tr
-                     else None})
+    roof = roofline(kernels, args.mode, _peaks())
     line = {"metric": METRIC, "value": t_scf, "unit": "s", "n_gpus": world, "steps": K,
             "warmup": args.warmup, "ms_per_step": t_iter * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.mode == "plain" else "f32+f64",
