@@ -23,6 +23,7 @@ FORGE_PREC_MIXED = 1
 FORGE_MIX_ODA, FORGE_MIX_PULAY = 0, 1
 FORGE_DEG_REFERENCE = 0
 FORGE_DEG_CORRECTED = 1
+FORGE_ERR_ARG = -1
 
 
 class ForgeError(RuntimeError):
@@ -120,6 +121,9 @@ SIGNATURES = {
     "forge_host_geometry": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "forge_host_run_scf": [_P, _P, _P, _P, _P],
     "forge_host_parameters_string": [_P, C.c_char_p, C.c_char_p, _I],
+    "forge_host_parameters_string_relax": [_P, C.c_char_p, _I, C.c_char_p, _I],
+    "forge_host_lattice_relaxation": [_P, _P, _P, _P, _P, _P, _P],
+    "forge_host_site_maps": [_P, _P, _P, _P, _P],
     "forge_host_plot_bands": [_P, _P, _D, _P, _P, _P, C.c_char_p],
     "forge_host_write_fock": [_P, _P, C.c_char_p, _I],
     "forge_host_read_fock": [_P, _P, C.c_char_p, _I],
@@ -205,6 +209,11 @@ class Setup:
     StepAlternative: float = 1.0
     degfactor_mode: str = "reference"
     precision: str = "fp64"
+    # Setup.f90:12: 1 relaxes bilayers (Main.f90:156-160) with the in-plane displacement table of this
+    # ntheta, relaxation = (uqx, uqy), each 5 x 5 with [n-1, m-1] = uqx(n, m)
+    # (forge_gb300.relaxation.read_displacement_table reads it from FORGE's Geometry.f90)
+    nrelax: int = 0
+    relaxation: Optional[tuple] = None
 
     def to_struct(self) -> forge_setup:
         s = forge_setup()
@@ -236,7 +245,8 @@ class Geometry:
 
 
 def build_geometry(setup: Setup) -> Geometry:
-    """Main.f90:102-163 through forge_host_geometry."""
+    """Main.f90:102-163 through forge_host_geometry; for nrelax = 1 and bilayers, LatticeRelaxation
+    (forge_host_lattice_relaxation) and then the C2 / C3 maps of the relaxed sites."""
     s = setup.to_struct()
     N, numk = s.ndim, s.numk
     Nk = numk * numk
@@ -252,6 +262,17 @@ def build_geometry(setup: Setup) -> Geometry:
         C.byref(s), _ptr(rl), _ptr(out.Coords), _ptr(out.nUnitCell_1), _ptr(out.nUnitCell_2), _ptr(out.tn),
         _ptr(out.g1), _ptr(out.g12), _ptr(out.MomentaValues), _ptr(out.nMomentaComponents),
         _ptr(out.nMomentaFlattened), _ptr(out.nC2pairs), _ptr(out.nC3pairs), _ptr(counts)))
+    if setup.nrelax == 1 and setup.nlayers == 2:
+        if setup.relaxation is None:
+            raise ForgeError(FORGE_ERR_ARG, "nrelax = 1 needs Setup.relaxation = (uqx, uqy), the displacement "
+                                            "table of this ntheta")
+        uqx, uqy = (_f(np.asarray(u, dtype=np.float64).reshape(5, 5), np.float64) for u in setup.relaxation)
+        matched = np.zeros(2, np.int64)
+        lib = load_library()
+        _check(lib.forge_host_lattice_relaxation(C.byref(s), _ptr(out.Coords), _ptr(out.g1), _ptr(out.g12),
+                                                 _ptr(uqx), _ptr(uqy), _ptr(matched)))
+        _check(lib.forge_host_site_maps(C.byref(s), _ptr(out.Coords), _ptr(out.nC2pairs), _ptr(out.nC3pairs),
+                                        _ptr(counts)))
     out.c2_count, out.c3_count = int(counts[0]), int(counts[1])
     return out
 
@@ -314,7 +335,8 @@ def fermi_2spins(setup: Setup, SortedEnergies_1Spin) -> dict:
 def parameters_string(setup: Setup, statename: str = "SSS") -> str:
     s = setup.to_struct()
     buf = C.create_string_buffer(256)
-    _check(load_library().forge_host_parameters_string(C.byref(s), statename.encode(), buf, 256))
+    _check(load_library().forge_host_parameters_string_relax(C.byref(s), statename.encode(), setup.nrelax, buf,
+                                                             256))
     return buf.value.decode()
 
 

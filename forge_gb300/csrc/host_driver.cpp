@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <string>
 #include <vector>
 
@@ -39,6 +40,127 @@ void rot(const double R[2][2], const double v[2], double out[2]) {
     double y = R[1][0] * v[0] + R[1][1] * v[1];
     out[0] = x;
     out[1] = y;
+}
+
+// C2 / C3 site maps (Geometry.f90:1140-1223) of N sites in L layers (Coords column-major N x 3).
+int site_maps(int64_t N, int64_t L, const double* Coords, int64_t* nC2pairs, int64_t* nC3pairs, int64_t* counts) {
+    const int64_t per = N / L;
+    int64_t c2cnt = 0, c3cnt = 0;
+    if (nC2pairs) {
+        for (int64_t i = 0; i < N; ++i) nC2pairs[i] = 0;
+        for (int64_t il = 1; il <= L; ++il)
+            for (int64_t i = per * (il - 1) + 1; i <= per * (il - 1) + per / 2; ++i)
+                for (int64_t j = per * (il - 1) + per / 2 + 1; j <= per * (il - 1) + per; ++j) {
+                    double dx = Coords[i - 1] + Coords[j - 1], dy = Coords[i - 1 + N] + Coords[j - 1 + N];
+                    if (std::sqrt(dx * dx + dy * dy) < 1e-5) {
+                        nC2pairs[i - 1] = j;
+                        nC2pairs[j - 1] = i;
+                        ++c2cnt;
+                    }
+                }
+    }
+    if (nC3pairs) {
+        for (int64_t i = 0; i < N; ++i) nC3pairs[i] = 0;
+        const double sq = std::sqrt(3.0);
+        for (int64_t nl = 1; nl <= L; ++nl) {
+            const int64_t base = (nl - 1) * per;
+            const int64_t lo[2] = {base + 1, base + per / 2 + 1}, hi[2] = {base + per / 2, base + per};
+            for (int h = 0; h < 2; ++h)
+                for (int64_t i = lo[h]; i <= hi[h]; ++i) {
+                    double x = Coords[i - 1], y = Coords[i - 1 + N];
+                    double x3 = -.5 * x - .5 * sq * y, y3 = .5 * sq * x - .5 * y;
+                    for (int64_t j = lo[h]; j <= hi[h]; ++j) {
+                        double dx = Coords[j - 1] - x3, dy = Coords[j - 1 + N] - y3;
+                        if (std::sqrt(dx * dx + dy * dy) < 1e-3) {
+                            nC3pairs[i - 1] = j;
+                            ++c3cnt;
+                        }
+                    }
+                }
+        }
+        for (int64_t nl = 1; nl <= L; ++nl) {
+            nC3pairs[(nl - 1) * per + per / 2 - 1] = (nl - 1) * per + per / 2;
+            nC3pairs[(nl - 1) * per + per - 1] = (nl - 1) * per + per;
+            c3cnt += 2;
+        }
+    }
+    if (counts) {
+        counts[0] = c2cnt;
+        counts[1] = c3cnt;
+    }
+    return 0;
+}
+
+// LatticeRelaxation (Geometry.f90:279-1135) of a bilayer of N sites, Coords column-major N x 3 in
+// place.  uqx, uqy: 5 x 5 column-major, uqx[(n-1) + 5 (m-1)] = uqx(n, m).  matched receives the two
+// layer-2 quarter counts (matches + 1, ndim/4 each when the re-indexing is a permutation).
+int lattice_relaxation(int64_t N, double* Coords, const double g1[2], const double g12[2], const double* uqx,
+                       const double* uqy, int64_t matched[2]) {
+    const double pi = pi_ref();
+    // Gn(1..8) of Geometry.f90:292-299
+    const double G[8][2] = {{g1[0], g1[1]},
+                            {g12[0], g12[1]},
+                            {g12[0] - g1[0], g12[1] - g1[1]},
+                            {-g1[0], -g1[1]},
+                            {-g12[0], -g12[1]},
+                            {-(g12[0] - g1[0]), -(g12[1] - g1[1])},
+                            {g1[0], g1[1]},
+                            {g12[0], g12[1]}};
+    // the 30 Fourier terms in the reference's summation order: nn = 1, 3, 5; n = 2..5; m = 1..n-1
+    struct Term {
+        double qx, qy, ux, uy;
+    };
+    std::vector<Term> terms;
+    for (int nn = 1; nn <= 5; nn += 2) {
+        const double ang = (double)(nn - 1) * pi / 3.0;
+        const double ca = std::cos(ang), sa = std::sin(ang);
+        for (int n = 2; n <= 5; ++n)
+            for (int m = 1; m < n; ++m) {
+                const double ux0 = uqx[(n - 1) + 5 * (m - 1)], uy0 = uqy[(n - 1) + 5 * (m - 1)];
+                terms.push_back({(double)(n - 1) * G[nn - 1][0] + (double)(m - 1) * G[nn + 1][0],
+                                 (double)(n - 1) * G[nn - 1][1] + (double)(m - 1) * G[nn + 1][1],
+                                 ca * ux0 - sa * uy0, sa * ux0 + ca * uy0});
+            }
+    }
+    const std::vector<double> nr(Coords, Coords + 3 * N);   // Coordsnr: the unrelaxed sites
+    const int64_t half = N / 2;
+    // layer 1 moves by delta / 2; layer 2 is its x-mirror (Geometry.f90:1058-1090)
+    for (int64_t i = 0; i < half; ++i) {
+        const double rx = Coords[i], ry = Coords[i + N];
+        double dx = 0.0, dy = 0.0;
+        for (const Term& t : terms) {
+            const double sv = std::sin(t.qx * rx + t.qy * ry);
+            dx = dx - 2.0 * t.ux * sv;
+            dy = dy - 2.0 * t.uy * sv;
+        }
+        Coords[i] = rx + dx / 2.0;
+        Coords[i + N] = ry + dy / 2.0;
+        Coords[i + half] = -Coords[i];
+        Coords[i + half + N] = Coords[i + N];
+    }
+    // re-index each layer-2 sublattice quarter onto the unrelaxed sites (Geometry.f90:1092-1132)
+    std::vector<double> tmp(3 * N, std::numeric_limits<double>::quiet_NaN());
+    for (int q = 0; q < 2; ++q) {
+        const int64_t lo = q == 0 ? half : 3 * N / 4, hi = q == 0 ? 3 * N / 4 : N;
+        int64_t cnt = 0;
+        for (int64_t i = lo; i < hi; ++i)
+            for (int64_t j = lo; j < hi; ++j) {
+                const double ex = Coords[i] - nr[j], ey = Coords[i + N] - nr[j + N];
+                if (std::sqrt(ex * ex + ey * ey) < 0.25) {
+                    ++cnt;
+                    for (int c = 0; c < 3; ++c) tmp[j + c * N] = Coords[i + c * N];
+                    break;
+                }
+            }
+        ++cnt;
+        tmp[hi - 1] = Coords[hi - 1];
+        tmp[hi - 1 + N] = -Coords[hi - 1 + N];
+        tmp[hi - 1 + 2 * N] = Coords[hi - 1 + 2 * N];
+        matched[q] = cnt;
+    }
+    for (int c = 0; c < 3; ++c)
+        for (int64_t j = half; j < N; ++j) Coords[j + c * N] = tmp[j + c * N];
+    return 0;
 }
 
 }  // namespace
@@ -205,52 +327,40 @@ int forge_host_geometry(const forge_setup* s, const int64_t* RotateLayers, doubl
     tn[3] = t2[1];
     tn[4] = t2[0] - t1[0];
     tn[5] = t2[1] - t1[1];
-    // C2 / C3 site maps (Geometry.f90:1140-1223)
-    const int64_t per = N / L;
-    int64_t c2cnt = 0, c3cnt = 0;
-    if (nC2pairs) {
-        for (int64_t i = 0; i < N; ++i) nC2pairs[i] = 0;
-        for (int64_t il = 1; il <= L; ++il)
-            for (int64_t i = per * (il - 1) + 1; i <= per * (il - 1) + per / 2; ++i)
-                for (int64_t j = per * (il - 1) + per / 2 + 1; j <= per * (il - 1) + per; ++j) {
-                    double dx = Coords[i - 1] + Coords[j - 1], dy = Coords[i - 1 + N] + Coords[j - 1 + N];
-                    if (std::sqrt(dx * dx + dy * dy) < 1e-5) {
-                        nC2pairs[i - 1] = j;
-                        nC2pairs[j - 1] = i;
-                        ++c2cnt;
-                    }
-                }
+    return site_maps(N, L, Coords, nC2pairs, nC3pairs, counts);
+}
+
+int forge_host_lattice_relaxation(const forge_setup* s, double* Coords, const double* g1, const double* g12,
+                                  const double* uqx, const double* uqy, int64_t* matched) {
+    if (!s || !Coords || !g1 || !g12 || !uqx || !uqy) {
+        forge::set_error(FORGE_ERR_ARG, "lattice_relaxation: null argument");
+        return FORGE_ERR_ARG;
     }
-    if (nC3pairs) {
-        for (int64_t i = 0; i < N; ++i) nC3pairs[i] = 0;
-        const double sq = std::sqrt(3.0);
-        for (int64_t nl = 1; nl <= L; ++nl) {
-            const int64_t base = (nl - 1) * per;
-            const int64_t lo[2] = {base + 1, base + per / 2 + 1}, hi[2] = {base + per / 2, base + per};
-            for (int h = 0; h < 2; ++h)
-                for (int64_t i = lo[h]; i <= hi[h]; ++i) {
-                    double x = Coords[i - 1], y = Coords[i - 1 + N];
-                    double x3 = -.5 * x - .5 * sq * y, y3 = .5 * sq * x - .5 * y;
-                    for (int64_t j = lo[h]; j <= hi[h]; ++j) {
-                        double dx = Coords[j - 1] - x3, dy = Coords[j - 1 + N] - y3;
-                        if (std::sqrt(dx * dx + dy * dy) < 1e-3) {
-                            nC3pairs[i - 1] = j;
-                            ++c3cnt;
-                        }
-                    }
-                }
-        }
-        for (int64_t nl = 1; nl <= L; ++nl) {
-            nC3pairs[(nl - 1) * per + per / 2 - 1] = (nl - 1) * per + per / 2;
-            nC3pairs[(nl - 1) * per + per - 1] = (nl - 1) * per + per;
-            c3cnt += 2;
-        }
+    if (s->nlayers != 2 || s->ndim < 8 || s->ndim % 4) {
+        forge::set_error(FORGE_ERR_ARG, "lattice_relaxation: bilayers only (nlayers = %lld, ndim = %lld)",
+                  (long long)s->nlayers, (long long)s->ndim);
+        return FORGE_ERR_ARG;
     }
-    if (counts) {
-        counts[0] = c2cnt;
-        counts[1] = c3cnt;
+    int64_t cnt[2] = {0, 0};
+    lattice_relaxation(s->ndim, Coords, g1, g12, uqx, uqy, cnt);
+    if (matched) {
+        matched[0] = cnt[0];
+        matched[1] = cnt[1];
+    }
+    if (cnt[0] != s->ndim / 4 || cnt[1] != s->ndim / 4) {
+        forge::set_error(FORGE_ERR_ARG,
+                  "lattice_relaxation: ERROR RELAXATION, layer-2 quarters matched %lld and %lld sites, expected %lld "
+                  "(unmatched sites are NaN)",
+                  (long long)cnt[0], (long long)cnt[1], (long long)(s->ndim / 4));
+        return FORGE_ERR_ARG;
     }
     return 0;
+}
+
+int forge_host_site_maps(const forge_setup* s, const double* Coords, int64_t* nC2pairs, int64_t* nC3pairs,
+                         int64_t* counts) {
+    if (!s || !Coords || s->nlayers < 1 || s->ndim % s->nlayers) return FORGE_ERR_ARG;
+    return site_maps(s->ndim, s->nlayers, Coords, nC2pairs, nC3pairs, counts);
 }
 
 int forge_host_plot_bands(const forge_setup* s, const double* Bands, double FermiEnergy,
@@ -290,17 +400,23 @@ int forge_host_plot_bands(const forge_setup* s, const double* Bands, double Ferm
     return 0;
 }
 
-int forge_host_parameters_string(const forge_setup* s, const char* statename, char* buf, int64_t buflen) {
-    if (!s || !buf || buflen < 8) return FORGE_ERR_ARG;
+int forge_host_parameters_string_relax(const forge_setup* s, const char* statename, int64_t nrelax, char* buf,
+                                       int64_t buflen) {
+    if (!s || !buf || buflen < 8 || nrelax < 0 || nrelax > 9) return FORGE_ERR_ARG;
     // Main.f90:180-183
     char dop = s->nfilling < 0.0 ? '-' : '+';
     std::snprintf(buf, (size_t)buflen,
-                  "-%.3s-filling%c%3.1f-numS%lld-i%lld-nlayers%lld-relax0-eps%.1f-U%4.2f-screen%lld-xi%.1f-delta%.3f"
+                  "-%.3s-filling%c%3.1f-numS%lld-i%lld-nlayers%lld-relax%lld-eps%.1f-U%4.2f-screen%lld-xi%.1f-delta%.3f"
                   "-numI%lld-numC%lld-numk%lld-dp8.dat",
                   statename ? statename : "SSS", dop, std::fabs(s->nfilling), (long long)s->numS,
-                  (long long)s->ntheta, (long long)s->nlayers, s->epsilon, s->U, (long long)s->nscreen,
-                  s->xi * 0.246, s->Delta, (long long)s->numI, (long long)s->numC, (long long)s->numk);
+                  (long long)s->ntheta, (long long)s->nlayers, (long long)nrelax, s->epsilon, s->U,
+                  (long long)s->nscreen, s->xi * 0.246, s->Delta, (long long)s->numI, (long long)s->numC,
+                  (long long)s->numk);
     return 0;
+}
+
+int forge_host_parameters_string(const forge_setup* s, const char* statename, char* buf, int64_t buflen) {
+    return forge_host_parameters_string_relax(s, statename, 0, buf, buflen);
 }
 
 // Fock checkpoint (Main.f90:647-672, 202-234): one complex value per fixed-length record

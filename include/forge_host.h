@@ -30,6 +30,24 @@ int forge_host_geometry(const forge_setup* s, const int64_t* RotateLayers, doubl
                         int64_t* nMomentaComponents, int64_t* nMomentaFlattened, int64_t* nC2pairs,
                         int64_t* nC3pairs, int64_t* counts);
 
+/* LatticeRelaxation (Geometry.f90:279-1135), called by Main.f90:156-160 for nrelax = 1 and bilayers,
+ * between the rotation of the sites and the C2 / C3 maps.  Coords (ndim x 3, column-major, the
+ * rotated sites of forge_host_geometry) is updated in place: layer 1 moves by half the displacement
+ * field sum of the 30 Fourier terms built from g1, g12 and the tables uqx, uqy (5 x 5, column-major:
+ * uqx[(n-1) + 5*(m-1)] = uqx(n, m); the reference hard-codes one table per ntheta = 2..35 at
+ * Geometry.f90:305-1056 and leaves other ntheta at zero), layer 2 becomes its x-mirror, re-indexed
+ * onto the unrelaxed layer-2 sites.  matched (2, may be NULL) receives the two layer-2 quarter counts.
+ * FORGE_ERR_ARG when nlayers != 2, or when a count is not ndim/4 (the reference's ERROR RELAXATION;
+ * the unmatched sites are then NaN, where the reference leaves them undefined). */
+int forge_host_lattice_relaxation(const forge_setup* s, double* Coords, const double* g1, const double* g12,
+                                  const double* uqx, const double* uqy, int64_t* matched);
+
+/* C2_RelatedPoints / C3_RelatedPoints (Geometry.f90:1140-1223) of the given sites: the 1-based maps
+ * nC2pairs / nC3pairs (ndim, may be NULL) and the two match counts (may be NULL).  Run after
+ * forge_host_lattice_relaxation, as Main.f90:162-163 does. */
+int forge_host_site_maps(const forge_setup* s, const double* Coords, int64_t* nC2pairs, int64_t* nC3pairs,
+                         int64_t* counts);
+
 typedef struct forge_scf_options {
     int64_t itmax;              /* Setup.f90:53 */
     double residual_tol;        /* > 0: stop once the mean-field residual is below it (eV) */
@@ -92,8 +110,11 @@ int forge_host_plot_bands(const forge_setup* s, const double* Bands, double Ferm
 int forge_host_write_fock(const forge_setup* s, const double* zFock, const char* path, int64_t record_bytes);
 int forge_host_read_fock(const forge_setup* s, double* zFock, const char* path, int64_t record_bytes);
 
-/* The parameter string of Main.f90:180-183 used in output file names. */
+/* The parameter string of Main.f90:180-183 used in output file names (nrelax 0); the _relax form
+ * takes Setup.f90:12's nrelax (0..9). */
 int forge_host_parameters_string(const forge_setup* s, const char* statename, char* buf, int64_t buflen);
+int forge_host_parameters_string_relax(const forge_setup* s, const char* statename, int64_t nrelax, char* buf,
+                                       int64_t buflen);
 
 #ifdef __cplusplus
 }

@@ -75,6 +75,11 @@ class Setup:
     nenforceC2T: int = 0
     nenforceValley: int = 0
     degfactor_mode: str = "reference"
+    # Setup.f90:12 nrelax: 1 applies LatticeRelaxation to bilayers (Main.f90:156-160) with the in-plane
+    # displacement table relax_uq = (uqx, uqy), 5 x 5 each, [n-1, m-1] holding uqx(n, m) of
+    # Geometry.f90:305-1056 for this ntheta (the reference hard-codes one table per ntheta = 2..35)
+    nrelax: int = 0
+    relax_uq: Optional[tuple] = None
 
     # derived (Setup.f90:10, 23-24, 58-69)
     @property
@@ -307,9 +312,77 @@ def build_geometry(s: Setup) -> Geometry:
     t1 = _rot(R, t1)
     t2 = _rot(R, t2)
     t3 = (t2[0] - t1[0], t2[1] - t1[1])
+    if s.nrelax == 1 and s.nlayers == 2:
+        if s.relax_uq is None:
+            raise ValueError("nrelax = 1 needs the displacement table relax_uq = (uqx, uqy) of this ntheta")
+        coords, matched = lattice_relaxation(s, coords, g1, g12, *s.relax_uq)
+        if matched != (s.ndim // 4, s.ndim // 4):
+            raise ValueError(f"LatticeRelaxation matched {matched} layer-2 sites, expected {s.ndim // 4} per quarter")
     c2, c2cnt = c2_related_points(s, coords)
     c3, c3cnt = c3_related_points(s, coords)
     return Geometry(coords, t1, t2, t3, g1, g12, u1, u2, kcomp, kflat, kvals, c2, c3, c2cnt, c3cnt)
+
+
+def lattice_relaxation(s: Setup, coords, g1, g12, uqx, uqy):
+    """LatticeRelaxation (Geometry.f90:279-1135) of a bilayer, on the rotated sites (Main.f90:156-160).
+
+    Layer 1 (sites 1..ndim/2): r += delta / 2 with
+        delta = -sum_{nn = 1, 3, 5} sum_{n = 2..5} sum_{m = 1..n-1} 2 R((nn-1) pi/3) u(n, m) sin(q . r),
+        q = (n-1) Gn(nn) + (m-1) Gn(nn+2),
+    Gn = (g1, g12, g12 - g1, -g1, -g12, g1 - g12, g1, g12) (Geometry.f90:292-299) and u(n, m) =
+    (uqx(n, m), uqy(n, m)) rotated by the angle (nn-1) pi/3 (Geometry.f90:1058-1085).
+    Layer 2 becomes the x-mirror (-x, y) of relaxed layer 1, keeping its z (Geometry.f90:1087-1088).
+    It is then re-indexed per sublattice quarter (Geometry.f90:1092-1132): for each site i of the
+    quarter, in order, the first site j of the same quarter whose UNRELAXED (x, y) lies within 0.25 a
+    of it takes its coordinates; the quarter's last site then takes (x, -y, z) of the mirrored site
+    stored at that index.  The reference prints ERROR RELAXATION when a quarter's count (matches + 1)
+    is not ndim/4, and leaves the unmatched sites undefined; here they are NaN.
+
+    uqx, uqy: 5 x 5, [n-1, m-1] = uqx(n, m).  Returns (coords, (count quarter 3, count quarter 4)).
+    """
+    N = s.ndim
+    c = np.array(coords, dtype=np.float64, copy=True)
+    nr = c.copy()
+    G = [tuple(g1), tuple(g12), (g12[0] - g1[0], g12[1] - g1[1])]
+    G += [(-v[0], -v[1]) for v in G] + [tuple(g1), tuple(g12)]
+    terms = []
+    for nn in (1, 3, 5):
+        ang = float(nn - 1) * PI / 3.0
+        ca, sa = math.cos(ang), math.sin(ang)
+        for n in range(2, 6):
+            for m in range(1, n):
+                qx = float(n - 1) * G[nn - 1][0] + float(m - 1) * G[nn + 1][0]
+                qy = float(n - 1) * G[nn - 1][1] + float(m - 1) * G[nn + 1][1]
+                ux = ca * uqx[n - 1][m - 1] - sa * uqy[n - 1][m - 1]
+                uy = sa * uqx[n - 1][m - 1] + ca * uqy[n - 1][m - 1]
+                terms.append((qx, qy, ux, uy))
+    half = N // 2
+    for i in range(half):
+        rx, ry = float(c[i, 0]), float(c[i, 1])
+        dx = dy = 0.0
+        for qx, qy, ux, uy in terms:
+            sq = math.sin(qx * rx + qy * ry)
+            dx = dx - 2.0 * ux * sq
+            dy = dy - 2.0 * uy * sq
+        c[i, 0] = rx + dx / 2.0
+        c[i, 1] = ry + dy / 2.0
+        c[i + half, 0] = -c[i, 0]
+        c[i + half, 1] = c[i, 1]
+    tmp = np.full_like(c, np.nan)
+    counts = []
+    for lo, hi in ((half, 3 * N // 4), (3 * N // 4, N)):
+        cnt = 0
+        for i in range(lo, hi):
+            d = np.sqrt((c[i, 0] - nr[lo:hi, 0]) ** 2 + (c[i, 1] - nr[lo:hi, 1]) ** 2)
+            hit = np.flatnonzero(d < 0.25)
+            if hit.size:
+                cnt += 1
+                tmp[lo + hit[0]] = c[i]
+        cnt += 1
+        tmp[hi - 1] = (c[hi - 1, 0], -c[hi - 1, 1], c[hi - 1, 2])
+        counts.append(cnt)
+    c[half:] = tmp[half:]
+    return c, tuple(counts)
 
 
 def c2_related_points(s: Setup, coords):
