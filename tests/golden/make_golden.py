@@ -54,7 +54,7 @@ def main(names=None):
     np.savez_compressed(os.path.join(HERE, "oracle_m1_k3.npz"), coords=r["geometry"].coords, LR=r["LR"], P=r["P"],
                         V=r["V"], E_in=np.array([l.E_in for l in r["logs"]]),
                         step=np.array([l.step for l in r["logs"]]), bands=r["bands"])
-    # config 0 (m=5, 6x6 k grid, charge neutrality): small derived quantities only
+    # the (5, 6) bilayer (m=5, 6x6 k grid, charge neutrality): small derived quantities only
     s = fo.Setup(ntheta=5, numk=6, itmax=3)
     r = fo.run_scf(s)
     rng = np.random.default_rng(0)

@@ -1,8 +1,8 @@
-"""Parity of the GPU SCF with the CPU oracle on the benchmark description's own workloads.
+"""Parity of the GPU SCF with the CPU oracle on the benchmark's two smaller workloads.
 
-- config 0: (5, 6) bilayer, N = 364, 6 x 6 k grid, charge neutrality, eps = 10, the reference's
+- the (5, 6) bilayer, N = 364, 6 x 6 k grid, charge neutrality, eps = 10, the reference's
   OptimalStep mixing and DegFactor rule, 30 SCF iterations (the configuration's count).
-- config 1: (10, 11) bilayer, N = 1324, 12 x 12 k grid (144 eigenproblems), nu = +2, eps = 10,
+- the (10, 11) bilayer, N = 1324, 12 x 12 k grid (144 eigenproblems), nu = +2, eps = 10,
   two FP64 iterations (the oracle takes about a minute per iteration on 16 cores).
 Tolerances as in test_gpu_parity.py: E/atom 1e-7 eV per iteration, P(R) 1e-8, window bands
 1e-9 eV, Fermi level 1e-9 eV, occupation counts and the heap-sort index maps exact; the order
@@ -54,7 +54,7 @@ def _check(so, reps, P, bands, idx, op, ref):
             assert abs(v - oref[k]) <= 1e-8 * max(1.0, abs(oref[k])), (k, v, oref[k])
 
 
-def test_config0_thirty_iterations_match_oracle(lib):
+def test_m5_bilayer_thirty_iterations_match_oracle(lib):
     import forge_gb300 as fg
     kw = dict(ntheta=5, numk=6, nfilling=0.0, epsilon=10.0)
     S = fg.Setup(**kw)
@@ -64,7 +64,7 @@ def test_config0_thirty_iterations_match_oracle(lib):
     _check(so, reps, P, bands, idx, op, ref)
 
 
-def test_config1_fp64_iterations_match_oracle(lib):
+def test_m10_bilayer_fp64_iterations_match_oracle(lib):
     import forge_gb300 as fg
     kw = dict(ntheta=10, numk=12, nfilling=2.0, epsilon=10.0)
     S = fg.Setup(**kw)

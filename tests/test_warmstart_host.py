@@ -1,7 +1,7 @@
 """Host logic of the learned warm start (forge_gb300.warmstart.apply), without a GPU.
 
-The benchmark spec's rule: the network's field is used only if its first residual beats the plain
-guess's, and the plain guess is the fallback otherwise.  A network that outputs NaN / Inf, or a
+The fallback rule of the learned start: the network's field is used only if its first residual beats
+the plain guess's, and the plain guess is the fallback otherwise.  A network that outputs NaN / Inf, or a
 residual comparison that is undefined (NaN), must also fall back, and the device must never see a
 non-finite field.  The device calls are replaced by a recording fake.
 """
