@@ -87,6 +87,7 @@ SIGNATURES = {
     "forge_gpu_get_fock": [_P, _D, _I, _I, _P],
     "forge_gpu_energies": [_P, _P, _P, _P, _P, _P],
     "forge_gpu_optimal_step": [_P, _P, _P],
+    "forge_gpu_energy_forms": [_P, _P, _P, _P],
     "forge_gpu_mix_potential": [_P, _D, _P, _P],
     "forge_gpu_plain_guess": [_P, _P],
     "forge_gpu_prepare_state": [_P, _P],
@@ -533,6 +534,24 @@ class HartreeFock:
         dn, res = C.c_double(), C.c_double()
         _check(self.lib.forge_gpu_mix_potential(self.ctx, Step, C.byref(dn), C.byref(res)))
         return dn.value, res.value
+
+    def EnergyForms(self):
+        """The energy forms of (P_in, P_new) after GetFock (forge_gpu_energy_forms): (forms[6], density of
+        P_in, density of P_new); the kinetic and Fock energies of (1-s) P_in + s P_new are
+        (1-s) forms[0] + s forms[1] and -((1-s)^2 forms[2] + 2 s (1-s) forms[3] + s^2 forms[4]) / 2."""
+        f = np.zeros(6)
+        d, dn = np.zeros(self.N), np.zeros(self.N)
+        _check(self.lib.forge_gpu_energy_forms(self.ctx, _ptr(f), _ptr(d), _ptr(dn)))
+        return f, d, dn
+
+    def Mix(self, Step: float):
+        """P = Step P_new + (1 - Step) P_in on the device (the OptimalStep mix of Main.f90:558-574): returns
+        (site densities of the mixed state, DensityConvergence).  The context's potential is the
+        numS = 1 one afterwards; a spin-polarised driver replaces it (SetPotential)."""
+        dn, _ = self.MixPotential(Step)
+        d = np.zeros(self.N)
+        _check(self.lib.forge_gpu_get_state(self.ctx, None, _ptr(d), None))
+        return d, dn
 
     def PlainGuess(self):
         E = np.zeros(4)

@@ -1885,6 +1885,32 @@ int forge_gpu_optimal_step(forge_ctx* x, double* Step, double* Energies) {
     return 0;
 }
 
+int forge_gpu_energy_forms(forge_ctx* x, double* forms, double* Density, double* DensityNew) {
+    FORGE_TRY(check_ctx(x));
+    Context& c = x->c;
+    if (!x->have_pnew || !forms) {
+        set_error(FORGE_ERR_STATE, "energy_forms needs get_fock first and a forms array");
+        return FORGE_ERR_STATE;
+    }
+    if (!c.lr_ready) FORGE_TRY(launch_long_range(c));
+    // the density of the current state (the mix measures the density change against it)
+    FORGE_TRY(scf_density(c, c.P.as<double2>(), c.dens.as<double>()));
+    FORGE_TRY(scf_density(c, x->Pn.as<double2>(), x->dens_new.as<double>()));
+    FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(),
+                               x->dens_new.as<double>(), x->y.as<double>(), x->work.as<double>(),
+                               x->sc.as<ScfScalars>()));
+    ScfScalars h;
+    FORGE_TRY(read_scalars(x, &h));
+    for (int t = 0; t < 6; ++t) forms[t] = h.forms[t];
+    if (Density)
+        FORGE_CUDA(cudaMemcpyAsync(Density, c.dens.ptr, c.N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    if (DensityNew)
+        FORGE_CUDA(
+            cudaMemcpyAsync(DensityNew, x->dens_new.ptr, c.N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    FORGE_CUDA(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
 int forge_gpu_mix_potential(forge_ctx* x, double Step, double* DensityConvergence, double* residual) {
     FORGE_TRY(check_ctx(x));
     Context& c = x->c;

@@ -12,8 +12,10 @@ host joins the spins:
 - it builds each spin's potential from both densities (Main.f90:586-594).
 
 The two spins' eigen-solves share one batched launch sequence (forge_gpu_solve_group over the two
-contexts).  Density matrices cross the host boundary once per energy evaluation.  This path is for
-correctness and for systems of moderate size; it is not the benchmarked path.
+contexts).  The density matrices stay on the device: each spin's context returns the energy forms
+of its (P_in, P_new) pair (forge_gpu_energy_forms), from which the host evaluates OptimalStep's
+three spin-summed energies, and mixes in place with the common step.  Per iteration only site
+densities, potentials, band energies and a few scalars cross the host boundary.
 
 Arrays follow the reference: zFock(ndim, ndim, numNeighborCells) per spin, column-major.
 """
@@ -92,10 +94,20 @@ class SpinPolarisedScf:
         self.hf = list(engines)
         self.LR = np.asarray(self.hf[0].LongRangeInteraction())
         self.hf[1].LongRangeInteraction(copy_out=False)
-        self.P = None
+        self._P = None          # host copies of the state, fetched on demand
+        self._have_state = False
         self.dens = None
         self.V = None
         self.E = None
+
+    @property
+    def P(self):
+        """Both spins' zFock (ndim, ndim, numNeighborCells), copied from the engines."""
+        if not self._have_state:
+            return None
+        if self._P is None:
+            self._P = [np.asfortranarray(h.GetState()[0]) for h in self.hf]
+        return self._P
 
     def close(self):
         if self._own:
@@ -108,16 +120,6 @@ class SpinPolarisedScf:
 
     def __exit__(self, *a):
         self.close()
-
-    # -- energies of a spin pair of density matrices (Main.f90:300-312, OptimalStep's evaluations)
-    def energies(self, P: Sequence[np.ndarray], dens: Sequence[np.ndarray]) -> tuple:
-        kin = fock = 0.0
-        for sp in range(2):
-            k, f, _, _ = self.hf[sp].Energies(P[sp])
-            kin += k
-            fock += f
-        eh, eu = hartree_hubbard(self.LR, dens)
-        return kin, fock, eh, eu
 
     def total(self, E: Sequence[float]) -> float:
         """TotalEnergy of Main.f90:312 with the factor 3 - numS = 1."""
@@ -134,11 +136,17 @@ class SpinPolarisedScf:
 
     def set_state(self, P: Sequence[np.ndarray]):
         """Loads both spins' zFock and forms their energies and potentials (Main.f90:294-346)."""
-        self.P = [np.asfortranarray(np.asarray(p, dtype=np.complex128)) for p in P]
+        P = [np.asfortranarray(np.asarray(p, dtype=np.complex128)) for p in P]
         for sp in range(2):
-            self.hf[sp].SetState(self.P[sp])
-        self.dens = [density(p) for p in self.P]
-        self.E = self.energies(self.P, self.dens)
+            self.hf[sp].SetState(P[sp])
+        self._P, self._have_state = P, True
+        self.dens = [density(p) for p in P]
+        kin = fock = 0.0
+        for sp in range(2):
+            k, f, _, _ = self.hf[sp].Energies()
+            kin += k
+            fock += f
+        self.E = (kin, fock) + hartree_hubbard(self.LR, self.dens)
         self.V = potentials(self.LR, self.dens, self.s.alphaH, self.s.U)
 
     def read_state(self, fock_dir: str, setup_in: Optional[Setup] = None, statename_in: str = "SSS",
@@ -154,7 +162,7 @@ class SpinPolarisedScf:
 
     # -- one SCF iteration (Main.f90:365-595)
     def iterate(self, it: int = 0) -> SpinIteration:
-        if self.P is None:
+        if not self._have_state:
             raise RuntimeError("no state: call plain_guess() or set_state() first")
         s = self.s
         sorted_e = []
@@ -177,16 +185,28 @@ class SpinPolarisedScf:
         fl = fermi_2spins(self.setup, np.stack(sorted_e, 1))
         deg = fl["DegFactor"]
         nocc, npart = fl["nOccStates"], fl["nPartOccStates"]
-        Pn = [self.hf[sp].GetFock(deg, nocc[sp], npart[sp]) for sp in range(2)]
+        for sp in range(2):
+            self.hf[sp].GetFock(deg, nocc[sp], npart[sp], copy_out=False)
         if self.setup.nenforceT or self.setup.nenforceC2 or self.setup.nenforceC2T:
             # Main.f90:513-534 on each spin's new zFock
-            Pn = [self.hf[sp].Symmetrize() for sp in range(2)]
-        dn_new = [density(p) for p in Pn]
-        # OptimalStep (HartreeFock.f90:1148-1227) over the spin-summed energy
+            for sp in range(2):
+                self.hf[sp].Symmetrize(copy_out=False)
+        # OptimalStep (HartreeFock.f90:1148-1227) over the spin-summed energy, from each spin's energy
+        # forms of (P_in, P_new): the kinetic energy is linear and the Fock energy quadratic in the step
+        forms = [self.hf[sp].EnergyForms() for sp in range(2)]
+
+        def energies_at(t: float) -> tuple:
+            u = 1.0 - t
+            kin = fock = 0.0
+            for f, _, _ in forms:
+                kin += u * f[0] + t * f[1]
+                fock += -0.5 * (u * u * f[2] + 2.0 * u * t * f[3] + t * t * f[4])
+            d = [u * din + t * dnew for _, din, dnew in forms]
+            return (kin, fock) + hartree_hubbard(self.LR, d)
+
         c0 = self.total(self.E)
-        t1 = self.total(self.energies(Pn, dn_new))
-        half = [0.5 * (self.P[sp] + Pn[sp]) for sp in range(2)]
-        t2 = self.total(self.energies(half, [0.5 * (self.dens[sp] + dn_new[sp]) for sp in range(2)]))
+        t1 = self.total(energies_at(1.0))
+        t2 = self.total(energies_at(0.5))
         c1 = 4.0 * t2 - t1 - 3.0 * c0
         c2 = t1 - c0 - c1
         if c2 > 0 and abs(-c1 / 2.0 / c2 - .5) < 0.5:
@@ -195,14 +215,13 @@ class SpinPolarisedScf:
             step = 1.0
         else:
             step = s.StepAlternative
-        P = [step * Pn[sp] + (1.0 - step) * self.P[sp] for sp in range(2)]
-        dens = [density(p) for p in P]
-        E = self.energies(P, dens)
-        dn = max(float(np.max(np.abs(dens[sp] - self.dens[sp]))) for sp in range(2))
+        mixed = [self.hf[sp].Mix(step) for sp in range(2)]
+        dens = [np.asarray(d) for d, _ in mixed]
+        dn = max(float(m) for _, m in mixed)
+        E = energies_at(step)[:2] + hartree_hubbard(self.LR, dens)
         Ein = self.E
-        self.P, self.dens, self.E = P, dens, E
-        for sp in range(2):
-            self.hf[sp].SetState(P[sp])
+        self._P = None
+        self.dens, self.E = dens, E
         self.V = potentials(self.LR, dens, s.alphaH, s.U)
         return SpinIteration(it, dn, step, self.total(Ein), self.total(E), fl["FermiEnergy"], tuple(nocc),
                              tuple(npart), deg, *Ein)
@@ -218,7 +237,7 @@ class SpinPolarisedScf:
         reference's record order (Main.f90:645-672)."""
         if P_init is not None:
             self.set_state(P_init)
-        elif self.P is None:
+        elif not self._have_state:
             self.plain_guess()
         params = parameters_string(self.setup, statename) if (output_dir or fock_dir) else ""
         fe = fc = None

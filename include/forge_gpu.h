@@ -169,6 +169,15 @@ int forge_gpu_energies(forge_ctx* ctx, const double* zFock, double* KineticEnerg
  * (Kinetic, Fock, Hartree, Hubbard) of P_in on entry and of the stepped state on exit. */
 int forge_gpu_optimal_step(forge_ctx* ctx, double* Step, double* Energies);
 
+/* The energy forms of the current state P_in and of P_new (after forge_gpu_get_fock), from which the
+ * kinetic and Fock energies of every mix (1-s) P_in + s P_new follow (OptimalStep's three
+ * evaluations, HartreeFock.f90:1148-1227, of one spin of a numS = 2 run): forms[0] = E_kin(P_in),
+ * forms[1] = E_kin(P_new), forms[2..4] = Q(P_in, P_in), Q(P_in, P_new), Q(P_new, P_new) with
+ * E_Fock(P) = -Q(P, P) / 2, forms[5] = max alpha |fv| |P_new - P_in| (6 doubles).  Density and
+ * DensityNew (N each, may be NULL) receive the site densities of P_in and P_new.  Nothing is mixed:
+ * forge_gpu_mix_potential with the chosen step follows. */
+int forge_gpu_energy_forms(forge_ctx* ctx, double* forms, double* Density, double* DensityNew);
+
 /* Main.f90:558-595: P = Step*P_new + (1-Step)*P_in, Density, DensityConvergence, Potential;
  * P_in <- P.  residual receives the mean-field residual (NULL allowed).  With FORGE_MIX_PULAY
  * (forge_gpu_set_mixing) the new state is the Anderson / Pulay mix of the history instead and

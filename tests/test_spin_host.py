@@ -64,6 +64,24 @@ class OracleSpinEngine:
         self.Pn = fo.enforce_symmetries(self.so, self.g, self.Pn)
         return _to_F(self.Pn)
 
+    def SetPotential(self, Potential):
+        self.V = np.asarray(Potential)
+
+    def EnergyForms(self):
+        # kinetic energy linear, Fock energy -Q(P, P) / 2 with Q a quadratic form
+        Q = lambda P: -2.0 * fo.fock_energy(self.so, self.T, P)   # noqa: E731
+        qa, qb = Q(self.P), Q(self.Pn)
+        qab = 0.5 * (Q(self.P + self.Pn) - qa - qb)
+        f = np.array([fo.kinetic_energy(self.so, self.T, self.P), fo.kinetic_energy(self.so, self.T, self.Pn),
+                      qa, qab, qb, 0.0])
+        return f, np.real(np.diagonal(self.P[0])).copy(), np.real(np.diagonal(self.Pn[0])).copy()
+
+    def Mix(self, Step):
+        d0 = np.real(np.diagonal(self.P[0])).copy()
+        self.P = Step * self.Pn + (1.0 - Step) * self.P
+        d = np.real(np.diagonal(self.P[0])).copy()
+        return d, float(np.max(np.abs(d - d0)))
+
 
 @pytest.mark.parametrize("split,flags", [(False, {}), (True, {}), (True, dict(nenforceT=1, nenforceC2=1)),
                                          (True, dict(nenforceValley=1))])
