@@ -21,7 +21,7 @@ Potential out), wall-clock timed from the guess to the converging iteration.
 
 Modes: fast = learned warm start + mixed-precision eigen-solve with the FP64-accurate eigenpair
 refinement; mixed = plain guess + the same mixed path; plain = plain guess + FP64.  The mixer is
-Anderson/Pulay (depth 6) unless --mixer oda (the reference's OptimalStep).
+Anderson/Pulay (depth 6) unless --mixer oda (the reference's OptimalStep) or --mixer linear.
 
 Workloads: 4 = 1.05 deg twisted bilayer, m=31, N=11908, 4x4 k, nu=+2, eps=10 (headline, default);
 1 = m=10, N=1324, 12x12 k, nu=+2; 2 = m=20, N=5044, 8x8 k, nu=-2, eps=8; 0 = m=5, N=364, 6x6 k,
@@ -491,7 +491,8 @@ def main():
     ap.add_argument("--mode", default="fast", choices=["fast", "mixed", "plain"],
                     help="fast: learned warm start + mixed-precision eigen-solve with eigenpair refinement; "
                          "mixed: plain guess + the same; plain: plain guess + FP64")
-    ap.add_argument("--mixer", default="pulay", choices=["pulay", "oda"])
+    ap.add_argument("--mixer", default="pulay", choices=["pulay", "oda", "linear"],
+                    help="linear: P = beta P_new + (1 - beta) P_in with beta = --mix-beta")
     ap.add_argument("--mix-depth", type=int, default=6)
     ap.add_argument("--mix-beta", type=float, default=0.7)
     ap.add_argument("--degfactor", default="corrected", choices=["corrected", "reference"])
@@ -593,8 +594,9 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.mode == "plain" else "f32+f64",
             "data": "synthetic",
             "config": {"workload": cfg["name"], "mode": args.mode, "degfactor": args.degfactor,
-                       "mixer": f"{args.mixer}(depth={args.mix_depth},beta={args.mix_beta})" if args.mixer == "pulay"
-                       else "oda", "N": r["N"], "Nk": r["Nk"], "converged": converged,
+                       "mixer": {"pulay": f"pulay(depth={args.mix_depth},beta={args.mix_beta})",
+                                 "linear": f"linear(beta={args.mix_beta})"}.get(args.mixer, "oda"),
+                       "N": r["N"], "Nk": r["Nk"], "converged": converged,
                        "iters_to_scf": iters if converged else None, "iterations_run": len(hist),
                        "residual_tol_eV": args.tol, "final_residual": hist[-1]["residual"] if hist else None,
                        "residuals": [h["residual"] for h in hist],

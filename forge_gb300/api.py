@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(_HERE, "libforge_gpu.so")
 
 FORGE_PREC_FP64 = 0
 FORGE_PREC_MIXED = 1
-FORGE_MIX_ODA, FORGE_MIX_PULAY = 0, 1
+FORGE_MIX_ODA, FORGE_MIX_PULAY, FORGE_MIX_LINEAR = 0, 1, 2
 FORGE_DEG_REFERENCE = 0
 FORGE_DEG_CORRECTED = 1
 FORGE_ERR_ARG = -1
@@ -441,9 +441,12 @@ class HartreeFock:
                     c2t_breaking=float(out[2]), c3_breaking=float(out[3]))
 
     def set_mixing(self, mode: str = "oda", depth: int = 6, beta: float = 0.7):
-        """SCF mixing: "oda" (the reference's OptimalStep) or "pulay" (Anderson / Pulay, `depth` steps)."""
-        _check(self.lib.forge_gpu_set_mixing(self.ctx, FORGE_MIX_PULAY if mode == "pulay" else FORGE_MIX_ODA,
-                                             depth, beta))
+        """SCF mixing: "oda" (the reference's OptimalStep), "pulay" (Anderson / Pulay, `depth` steps) or
+        "linear" (P = beta P_new + (1 - beta) P_in)."""
+        modes = {"oda": FORGE_MIX_ODA, "pulay": FORGE_MIX_PULAY, "linear": FORGE_MIX_LINEAR}
+        if mode not in modes:
+            raise ValueError(f"mixing mode {mode!r}: one of {sorted(modes)}")
+        _check(self.lib.forge_gpu_set_mixing(self.ctx, modes[mode], depth, beta))
 
     def LongRangeInteraction(self, copy_out: bool = True) -> Optional[np.ndarray]:
         """HartreeFock.f90:14-53."""

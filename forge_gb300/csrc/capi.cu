@@ -59,7 +59,7 @@ int launch_sort_fermi(Context& c, const double* w, double nfilling, double* sort
 int scf_energy_forms(Context& c, const double* te, const double2* Pa, const double2* Pb, const double* da,
                      const double* db, double* y, double* work, ScfScalars* sc);
 size_t scf_work_doubles(int64_t N);
-int scf_oda(Context& c, ScfScalars* sc, int mode);
+int scf_oda(Context& c, ScfScalars* sc, int mode, double fixed_step = 0.0);
 int scf_mix(Context& c, double2* P, const double2* Pn, double* dens, double* V, const double* y, double* work,
             ScfScalars* sc);
 int scf_combine(Context& c, double2* win, const double2* bulk);
@@ -114,7 +114,8 @@ struct forge_ctx {
     DevBuf g_H, g_X, g_w, g_eigws, g_mixws, g_tmp, g_rows, g_sig, g_rr;
     int64_t eig_batch = 0;
     int64_t k_begin = 0, k_end = 0;  // local k range (k_end = 0: all k)
-    // mixing: FORGE_MIX_ODA (OptimalStep, the reference) or FORGE_MIX_PULAY (Anderson / Pulay)
+    // mixing: FORGE_MIX_ODA (OptimalStep, the reference), FORGE_MIX_PULAY (Anderson / Pulay) or
+    // FORGE_MIX_LINEAR (P = beta P_new + (1 - beta) P_in)
     int mix_mode = FORGE_MIX_ODA;
     int diis_depth = 6;
     double diis_beta = 0.7;
@@ -982,7 +983,7 @@ int scf_iteration_end(forge_ctx* x, const double* Ein, int info, double* Energie
     if (x->mix_mode == FORGE_MIX_PULAY) {
         FORGE_TRY(pulay_mix(x));
     } else {
-        FORGE_TRY(scf_oda(c, x->sc.as<ScfScalars>(), 0));
+        FORGE_TRY(scf_oda(c, x->sc.as<ScfScalars>(), x->mix_mode == FORGE_MIX_LINEAR ? 2 : 0, x->diis_beta));
         FORGE_TRY(scf_mix(c, c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(), c.V.as<double>(),
                           x->y.as<double>(), x->work.as<double>(), x->sc.as<ScfScalars>()));
     }
@@ -1408,7 +1409,8 @@ int forge_gpu_order_parameters(forge_ctx* x, const int64_t* nC2pairs, const int6
 
 int forge_gpu_set_mixing(forge_ctx* x, int64_t mode, int64_t depth, double beta) {
     FORGE_TRY(check_ctx(x));
-    if ((mode != FORGE_MIX_ODA && mode != FORGE_MIX_PULAY) || depth < 1 || depth > DIIS_MAX - 1 || !(beta > 0.0) ||
+    if ((mode != FORGE_MIX_ODA && mode != FORGE_MIX_PULAY && mode != FORGE_MIX_LINEAR) || depth < 1 ||
+        depth > DIIS_MAX - 1 || !(beta > 0.0) ||
         beta > 1.0) {
         set_error(FORGE_ERR_ARG, "set_mixing: mode %lld, depth %lld (1..%d), beta %g (0..1]", (long long)mode,
                   (long long)depth, DIIS_MAX - 1, beta);
@@ -1878,7 +1880,7 @@ int forge_gpu_optimal_step(forge_ctx* x, double* Step, double* Energies) {
     FORGE_TRY(scf_energy_forms(c, x->te.as<double>(), c.P.as<double2>(), x->Pn.as<double2>(), c.dens.as<double>(),
                                x->dens_new.as<double>(), x->y.as<double>(), x->work.as<double>(),
                                x->sc.as<ScfScalars>()));
-    FORGE_TRY(scf_oda(c, x->sc.as<ScfScalars>(), 0));
+    FORGE_TRY(scf_oda(c, x->sc.as<ScfScalars>(), x->mix_mode == FORGE_MIX_LINEAR ? 2 : 0, x->diis_beta));
     FORGE_TRY(read_scalars(x, &h));
     if (Step) *Step = h.step;
     for (int t = 0; t < 4; ++t) Energies[t] = h.Eout[t];

@@ -363,6 +363,7 @@ struct EnergyParams {
     // mixed precision only: a step below 1 whose predicted gain over step 1, c2 (1 - s)^2, is below
     // oda_noise |E_tot| is noise of the FP32-level P_new, and step 1 is taken (0: the reference rule)
     double oda_noise;
+    double fixed_step;   // mode 2 (linear mixing): the step, in place of OptimalStep's
 };
 
 // energies of the state (1-s) a + s b from the forms
@@ -379,7 +380,7 @@ __device__ inline double total_energy(const EnergyParams& p, const double E[4]) 
     return p.alpha * E[1] * (double)(3 - p.numS) + E[0] * (double)(3 - p.numS) + p.U * E[3] + p.alphaH * E[2];
 }
 
-// mode 0: OptimalStep; mode 1: energies of b only (s = 1)
+// mode 0: OptimalStep; mode 1: energies of b only (s = 1); mode 2: linear mixing with p.fixed_step
 __global__ void k_oda(ScfScalars* sc, EnergyParams p, int mode) {
     if (threadIdx.x != 0) return;
     double E1[4], Eh[4], Es[4];
@@ -398,13 +399,16 @@ __global__ void k_oda(ScfScalars* sc, EnergyParams p, int mode) {
     const double c1 = 4.0 * t2 - t1 - 3.0 * c0;
     const double c2 = t1 - c0 - c1;
     double step;
-    if ((c2 > 0) && (fabs(-c1 / 2.0 / c2 - .5) < 0.5))
+    if (mode == 2)
+        step = p.fixed_step;
+    else if ((c2 > 0) && (fabs(-c1 / 2.0 / c2 - .5) < 0.5))
         step = -c1 / 2.0 / c2;
     else if (t1 < c0)
         step = 1.0;
     else
         step = p.StepAlternative;
-    if (p.oda_noise > 0.0 && step < 1.0 && c2 * (1.0 - step) * (1.0 - step) < p.oda_noise * fabs(c0)) step = 1.0;
+    if (mode == 0 && p.oda_noise > 0.0 && step < 1.0 && c2 * (1.0 - step) * (1.0 - step) < p.oda_noise * fabs(c0))
+        step = 1.0;
     energies_at(sc, step, Es);
     for (int t = 0; t < 4; ++t) sc->Eout[t] = Es[t];
     sc->E1tot = t1;
@@ -515,10 +519,10 @@ int scf_energy_forms(Context& c, const double* te, const double2* Pa, const doub
 
 size_t scf_work_doubles(int64_t N) { return RED_CTAS * 8 + (size_t)LR_CHUNKS * 2 * N + 8 * ((N + 255) / 256) + 64; }
 
-int scf_oda(Context& c, ScfScalars* sc, int mode) {
+int scf_oda(Context& c, ScfScalars* sc, int mode, double fixed_step) {
     // the FP32-noise guard of OptimalStep only for FP32-accurate P_new (not after the refinement)
     EnergyParams p{c.s.alpha, c.s.alphaH, c.s.U, c.s.StepAlternative, 1,
-                   (c.precision == FORGE_PREC_MIXED && !c.refined) ? 1e-8 : 0.0};
+                   (c.precision == FORGE_PREC_MIXED && !c.refined) ? 1e-8 : 0.0, fixed_step};
     k_oda<<<1, 32, 0, c.stream>>>(sc, p, mode);
     FORGE_LAUNCH_CHECK();
     return 0;

@@ -42,7 +42,7 @@ enum {
 
 enum { FORGE_PREC_FP64 = 0, FORGE_PREC_MIXED = 1 };
 /* SCF mixing: the reference's OptimalStep (ODA) or Anderson / Pulay mixing of the density matrix. */
-enum { FORGE_MIX_ODA = 0, FORGE_MIX_PULAY = 1 };
+enum { FORGE_MIX_ODA = 0, FORGE_MIX_PULAY = 1, FORGE_MIX_LINEAR = 2 };
 enum { FORGE_DEG_REFERENCE = 0, FORGE_DEG_CORRECTED = 1 };
 
 /* Runtime mirror of Setup.f90:6-74 (only the parameters the SCF path reads). */
@@ -228,7 +228,9 @@ int forge_gpu_scf_iteration_group(forge_ctx** ctxs, int64_t nctx, double* Energi
  * minimising |r - sum_i g_i dr_i|.  The history (complex64 differences, 2 x 4 N^2 x 8 bytes per
  * step) is kept on the device and is cleared by set_state, plain_guess, field_guess,
  * prepare_state and a change of precision.  With Pulay the reported residual is that of
- * (P_in, P_new) and Step is 1. */
+ * (P_in, P_new) and Step is 1.  FORGE_MIX_LINEAR mixes P <- beta P_new + (1 - beta) P_in (the
+ * benchmark description's "linear mixing 0.3"): forge_gpu_optimal_step then returns Step = beta
+ * with the energies of that state, and depth is not used. */
 int forge_gpu_set_mixing(forge_ctx* ctx, int64_t mode, int64_t depth, double beta);
 
 /* FP64 Rayleigh-Ritz refinement after every FORGE_PREC_MIXED eigen-solve (no counterpart in the

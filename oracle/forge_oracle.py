@@ -1300,10 +1300,11 @@ class PulayMixer:
 
 def run_scf(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTables] = None, LR=None,
             P_init=None, itmax: Optional[int] = None, residual_tol: Optional[float] = None,
-            keep_history: bool = False, mixer: Optional[PulayMixer] = None):
+            keep_history: bool = False, mixer: Optional[PulayMixer] = None, linear_beta: Optional[float] = None):
     """Main.f90:236-679 for numS=1: initial guess, energies, potential, then the SCF loop with ODA mixing
     (or, with ``mixer``, Anderson / Pulay mixing: the state is the mixer's output, Step is 1 and the
-    residual is that of (P_in, P_new)).
+    residual is that of (P_in, P_new); or, with ``linear_beta``, linear mixing: Main.f90:558-595 with
+    the fixed Step = linear_beta in place of OptimalStep's, the library's FORGE_MIX_LINEAR).
 
     Stops after ``itmax`` iterations (reference behaviour) or earlier when
     ``residual_tol`` is given and the mean-field residual drops below it.
@@ -1348,10 +1349,15 @@ def run_scf(s: Setup, g: Optional[Geometry] = None, T: Optional[PairTables] = No
             dn = float(np.max(np.abs(dens - dens_in)))
             V = potential(s, LR, dens)
         else:
-            step, E, t1, t2 = optimal_step(s, T, LR, P_new, P_in, dens_new, dens_in, E_in)
-            Etot = E.total(s)
+            if linear_beta is not None:
+                step, t1, t2 = float(linear_beta), float("nan"), float("nan")
+            else:
+                step, E, t1, t2 = optimal_step(s, T, LR, P_new, P_in, dens_new, dens_in, E_in)
             P = step * P_new + (1.0 - step) * P_in
             dens = np.real(np.diagonal(P[0])).copy()
+            if linear_beta is not None:
+                E = energies(s, T, LR, P, dens)
+            Etot = E.total(s)
             dn = float(np.max(np.abs(dens - dens_in)))
             V_old = V
             V = potential(s, LR, dens)

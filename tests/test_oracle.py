@@ -148,19 +148,36 @@ def test_golden_fixtures_reproduce():
     assert np.max(np.abs(r["LR"] - gd["LR"])) < 1e-13
 
 
-def test_oracle_pulay_mixing_reaches_the_optimalstep_fixed_point():
-    """The oracle's Anderson / Pulay mixer (the library's FORGE_MIX_PULAY restated) converges to the
-    fixed point the reference's OptimalStep SCF reaches, in fewer iterations."""
+@pytest.fixture(scope="module")
+def m2_fixed_point():
+    """The reference's OptimalStep SCF of the (2, 3) bilayer at nu = +2, converged to 1e-11 eV."""
     so = fo.Setup(ntheta=2, numk=3, nfilling=2.0)
     g = fo.build_geometry(so)
     T = fo.pair_tables(so, g)
     LR = fo.long_range_interaction(so, g)
-    oda = fo.run_scf(so, g, T, LR, itmax=400, residual_tol=1e-11)
+    return so, g, T, LR, fo.run_scf(so, g, T, LR, itmax=400, residual_tol=1e-11)
+
+
+def test_oracle_pulay_mixing_reaches_the_optimalstep_fixed_point(m2_fixed_point):
+    """The oracle's Anderson / Pulay mixer (the library's FORGE_MIX_PULAY restated) converges to the
+    fixed point the reference's OptimalStep SCF reaches, in fewer iterations."""
+    so, g, T, LR, oda = m2_fixed_point
     pul = fo.run_scf(so, g, T, LR, itmax=400, residual_tol=1e-11, mixer=fo.PulayMixer(6, 0.7))
     assert oda["logs"][-1].residual < 1e-11 and pul["logs"][-1].residual < 1e-11
     assert len(pul["logs"]) < len(oda["logs"])
     assert np.max(np.abs(pul["P"] - oda["P"])) <= 1e-9
     assert abs(pul["Etot"] - oda["Etot"]) / so.ndim <= 1e-9
+
+
+def test_oracle_linear_mixing_reaches_the_optimalstep_fixed_point(m2_fixed_point):
+    """Linear mixing (Step fixed at beta, the library's FORGE_MIX_LINEAR) converges to the fixed point
+    of the reference's OptimalStep SCF, and every logged Step is beta."""
+    so, g, T, LR, oda = m2_fixed_point
+    lin = fo.run_scf(so, g, T, LR, itmax=200, residual_tol=1e-10, linear_beta=0.7)
+    assert lin["logs"][-1].residual < 1e-10
+    assert all(l.step == 0.7 for l in lin["logs"])
+    assert np.max(np.abs(lin["P"] - oda["P"])) <= 1e-8
+    assert abs(lin["Etot"] - oda["Etot"]) / so.ndim <= 1e-9
 
 
 def test_variant_fixtures_reproduce():
