@@ -115,6 +115,25 @@ def test_trace_and_storage_invariants(scf_m2):
     assert np.max(np.abs(P[0] - P[0].conj().T)) < 1e-12
 
 
+def test_zheevr_oracle_agrees_with_zheevd(scf_m2):
+    """The oracle's eigen-solver is the reference's zheevr (range 'I', 'L' triangle); the FP64 result
+    the benchmark description names is LAPACK's zheevd.  On H(k) of an SCF state the two agree:
+    eigenvalues 1..nUpper to 1e-12 eV and the projector onto bands 1..nLower-1 to 1e-12."""
+    from scipy.linalg import lapack
+    s, r = scf_m2
+    g, T = r["geometry"], r["tables"]
+    for icount in (0, 4):
+        H = fo.hamiltonian(s, g, T, r["V"], r["P"], g.vk(icount))
+        w_r, z_r = fo.eigh_lower(H, s.nUpper)
+        w_d, z_d, info = lapack.zheevd(H, compute_v=1, lower=1)
+        assert info == 0
+        assert np.max(np.abs(w_r - w_d[:s.nUpper])) <= 1e-12
+        k = s.nLower - 1
+        P_r = z_r[:, :k] @ z_r[:, :k].conj().T
+        P_d = z_d[:, :k] @ z_d[:, :k].conj().T
+        assert np.max(np.abs(P_r - P_d)) <= 1e-12
+
+
 def test_hamiltonian_hermitian_lower_triangle(scf_m2):
     s, r = scf_m2
     g, T = r["geometry"], r["tables"]
