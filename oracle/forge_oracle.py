@@ -386,25 +386,31 @@ def lattice_relaxation(s: Setup, coords, g1, g12, uqx, uqy):
 
 
 def c2_related_points(s: Setup, coords):
-    """Geometry.f90:1140-1167 (1-based map, count)."""
+    """Geometry.f90:1140-1167 (1-based map, count).  The pair distances of a layer are evaluated as
+    one array (the same IEEE operations as the reference's scalar loop); the matches are then applied
+    in the loop's (i, j) order, so repeated matches resolve as in the reference."""
     N, L = s.ndim, s.nlayers
+    X = np.asarray(coords, dtype=np.float64)
     pairs = np.zeros(N, dtype=np.int64)
     cnt = 0
     per = N // L
-    for il in range(1, L + 1):
-        for i in range(per * (il - 1) + 1, per * (il - 1) + per // 2 + 1):
-            for j in range(per * (il - 1) + per // 2 + 1, per * (il - 1) + per + 1):
-                r = math.sqrt((coords[i - 1, 0] + coords[j - 1, 0]) ** 2 + (coords[i - 1, 1] + coords[j - 1, 1]) ** 2)
-                if r < 1e-5:
-                    pairs[i - 1] = j
-                    pairs[j - 1] = i
-                    cnt += 1
+    for il in range(L):
+        a0, b0 = per * il, per * il + per // 2
+        xi, yi = X[a0:b0, 0][:, None], X[a0:b0, 1][:, None]
+        xj, yj = X[b0:a0 + per, 0][None, :], X[b0:a0 + per, 1][None, :]
+        r = np.sqrt((xi + xj) ** 2 + (yi + yj) ** 2)
+        for i, j in zip(*np.nonzero(r < 1e-5)):
+            pairs[a0 + i] = b0 + j + 1
+            pairs[b0 + j] = a0 + i + 1
+            cnt += 1
     return pairs, cnt
 
 
 def c3_related_points(s: Setup, coords):
-    """Geometry.f90:1172-1223 (1-based map, count)."""
+    """Geometry.f90:1172-1223 (1-based map, count), with the distances of a sublattice block as one
+    array and the matches applied in the reference's loop order (the last match of a site wins)."""
     N, L = s.ndim, s.nlayers
+    X = np.asarray(coords, dtype=np.float64)
     per = N // L
     pairs = np.zeros(N, dtype=np.int64)
     cnt = 0
@@ -412,15 +418,13 @@ def c3_related_points(s: Setup, coords):
     for nl in range(1, L + 1):
         base = (nl - 1) * per
         for lo, hi in ((base + 1, base + per // 2), (base + per // 2 + 1, base + per)):
-            for i in range(lo, hi + 1):
-                x, y = coords[i - 1, 0], coords[i - 1, 1]
-                x3 = -.5 * x - .5 * sq * y
-                y3 = .5 * sq * x - .5 * y
-                for j in range(lo, hi + 1):
-                    r = math.sqrt((coords[j - 1, 0] - x3) ** 2 + (coords[j - 1, 1] - y3) ** 2)
-                    if r < 1e-3:
-                        pairs[i - 1] = j
-                        cnt += 1
+            x, y = X[lo - 1:hi, 0], X[lo - 1:hi, 1]
+            x3 = -.5 * x - .5 * sq * y
+            y3 = .5 * sq * x - .5 * y
+            r = np.sqrt((x[None, :] - x3[:, None]) ** 2 + (y[None, :] - y3[:, None]) ** 2)
+            for i, j in zip(*np.nonzero(r < 1e-3)):
+                pairs[lo - 1 + i] = lo + j
+                cnt += 1
     for nl in range(1, L + 1):
         pairs[(nl - 1) * per + per // 2 - 1] = (nl - 1) * per + per // 2
         pairs[(nl - 1) * per + per - 1] = (nl - 1) * per + per
