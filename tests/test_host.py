@@ -27,6 +27,15 @@ def test_library_exports_every_declared_symbol(lib):
         assert hasattr(lib, name), name
 
 
+def test_fortran_binding_declares_every_device_entry():
+    """The Fortran module written out for a FORGE host binds every entry point of forge_gpu.h, by
+    its C name (bind(C, name=...))."""
+    txt = open(os.path.join(ROOT, "include", "forge_gpu.h")).read()
+    device = set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(forge_gpu_\w+)\s*\(", txt, flags=re.M))
+    bound = set(re.findall(r'bind\(C, name="(forge_\w+)"\)', open(os.path.join(ROOT, "INTEGRATION.md")).read()))
+    assert device and device <= bound, sorted(device - bound)
+
+
 def test_library_calls_fail_cleanly_without_context(lib):
     # argument checks run before any device work
     assert lib.forge_gpu_solve(None, None, None, None, None, None) < 0
