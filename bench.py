@@ -360,6 +360,11 @@ def run_ours(args, cfg):
     run = scf_device(hf, S, args, args.steps, args.budget_s, t_wall0, profile=True)
     clk = clocks.stop()
     hf.profile(False)
+    # order parameters of the state the timed SCF ended on (device reduction over P(0))
+    try:
+        run["order_parameters"] = hf.OrderParameters()
+    except Exception as e:  # a diagnostic: its failure must not cost the measured line
+        run["order_parameters"] = {"error": str(e)}
     state = None
     if args.save_state:
         state = _state_summary(hf, S)
@@ -602,6 +607,8 @@ def main():
                        "residuals": [h["residual"] for h in hist],
                        "refined": [h["refined"] for h in hist],
                        "energies": [h["TotalEnergy"] for h in hist],
+                       "energy_per_atom": hist[-1]["TotalEnergy"] / r["N"] if hist else None,
+                       "order_parameters": run.get("order_parameters"),
                        "guess_s": run["t_guess"], "setup_s": r["t_setup"], **run["guess_info"],
                        "value_source": "CUDA events of this run: start of the guess to the end of the first "
                                        "iteration below the residual tolerance",
