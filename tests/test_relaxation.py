@@ -147,3 +147,27 @@ def test_parameters_string_carries_nrelax():
     import forge_gb300 as fg
     assert "-relax1-" in fg.parameters_string(fg.Setup(ntheta=2, numk=2, nrelax=1, relaxation=_uq(2)))
     assert "-relax0-" in fg.parameters_string(fg.Setup(ntheta=2, numk=2))
+
+
+def test_host_relaxation_entry_checks_its_arguments(lib):
+    """The C entries reject null arguments, non-bilayers and bad nrelax before touching memory."""
+    import ctypes as C
+    import forge_gb300 as fg
+    S = fg.Setup(ntheta=2, numk=2)
+    s = S.to_struct()
+    N = s.ndim
+    X = np.zeros((N, 3), order="F")
+    g = np.zeros(2)
+    u = np.zeros((5, 5), order="F")
+    p = lambda a: a.ctypes.data_as(C.c_void_p)   # noqa: E731
+    assert lib.forge_host_lattice_relaxation(C.byref(s), None, p(g), p(g), p(u), p(u), None) == -1
+    assert lib.forge_host_lattice_relaxation(None, p(X), p(g), p(g), p(u), p(u), None) == -1
+    s3 = fg.Setup(ntheta=2, nlayers=3, RotateLayers=(-1, 1, -1), numk=2).to_struct()
+    X3 = np.zeros((s3.ndim, 3), order="F")
+    assert lib.forge_host_lattice_relaxation(C.byref(s3), p(X3), p(g), p(g), p(u), p(u), None) == -1
+    assert b"bilayers only" in lib.forge_gpu_last_error()
+    assert lib.forge_host_site_maps(C.byref(s), None, None, None, None) == -1
+    buf = C.create_string_buffer(256)
+    assert lib.forge_host_parameters_string_relax(C.byref(s), b"SSS", 10, buf, 256) == -1
+    assert lib.forge_host_parameters_string_relax(C.byref(s), b"SSS", 1, buf, 256) == 0
+    assert b"-relax1-" in buf.value
